@@ -1,0 +1,185 @@
+// Grid-index kernels: per-dimension extent, cell id per point, gather of the
+// points into cell order, the cell table and the work items of the query kernels.
+// Reference: spatial_index.h:92-216 (SpatialIndex constructor path).
+#pragma once
+
+#include <cfloat>
+#include <climits>
+
+#include "hpd_common.cuh"
+
+namespace hpd {
+
+// --------------------------------------------------------------- element traits
+// F: the floating type of (x - min) / eps in the reference expression
+// (double for double points, float for everything else: the integer difference is
+// converted to float because eps is a float).
+template <typename T> struct Elem;
+template <> struct Elem<float> {
+    using F = float;
+    static constexpr bool kFloat = true;
+    __host__ __device__ static float lowest_for_max() { return FLT_MIN; }  // numeric_limits<float>::min()
+    __host__ __device__ static float highest() { return FLT_MAX; }
+};
+template <> struct Elem<double> {
+    using F = double;
+    static constexpr bool kFloat = true;
+    __host__ __device__ static double lowest_for_max() { return DBL_MIN; }
+    __host__ __device__ static double highest() { return DBL_MAX; }
+};
+
+// (x - mn) as the reference evaluates it, in the float type F.
+template <typename T>
+__host__ __device__ __forceinline__ typename Elem<T>::F diff_f(T x, T mn) {
+#ifdef __CUDA_ARCH__
+    return sub_(x, mn);
+#else
+    return x - mn;  // host code is compiled without contraction or fast-math
+#endif
+}
+
+// floor((x - mn) / eps) with the reference's rounding, as an unsigned cell index.
+template <typename T>
+__device__ __forceinline__ unsigned long long cell_coord(T x, T mn, typename Elem<T>::F eps, typename Elem<T>::F recip,
+                                                         int cell_mode) {
+    using F = typename Elem<T>::F;
+    F df = diff_f<T>(x, mn);
+    F q;
+    if (cell_mode == HPD_CELL_RECIP) {
+        if (sizeof(F) == 4) q = (F)__fmul_rn((float)df, (float)recip);
+        else q = (F)__dmul_rn((double)df, (double)recip);
+    } else {
+        if (sizeof(F) == 4) q = (F)__fdiv_rn((float)df, (float)eps);
+        else q = (F)__ddiv_rn((double)df, (double)eps);
+    }
+    if (sizeof(F) == 4) return (unsigned long long)floorf((float)q);
+    return (unsigned long long)floor((double)q);
+}
+
+// ---------------------------------------------------------------- min / max
+// Threads of a block are laid out so that thread t always reads dimension t % d:
+// the block size and the grid stride are multiples of d.
+template <typename T>
+__global__ void k_minmax_partial(const T* __restrict__ data, int64_t count, int d, T* __restrict__ pmin,
+                                 T* __restrict__ pmax, int* __restrict__ bad) {
+    extern __shared__ unsigned char smem_raw[];
+    T* smin = reinterpret_cast<T*>(smem_raw);
+    T* smax = smin + blockDim.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    T mn = Elem<T>::highest(), mx = -Elem<T>::highest();
+    bool nonfinite = false;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += stride) {
+        T c = data[e];
+        if (Elem<T>::kFloat && !isfinite(c)) nonfinite = true;
+        if (c < mn) mn = c;
+        if (mx < c) mx = c;
+    }
+    if (nonfinite) atomicExch(bad, 1);
+    smin[threadIdx.x] = mn;
+    smax[threadIdx.x] = mx;
+    __syncthreads();
+    if (threadIdx.x < (unsigned)d) {
+        for (int t = threadIdx.x + d; t < (int)blockDim.x; t += d) {
+            if (smin[t] < mn) mn = smin[t];
+            if (mx < smax[t]) mx = smax[t];
+        }
+        pmin[(int64_t)blockIdx.x * d + threadIdx.x] = mn;
+        pmax[(int64_t)blockIdx.x * d + threadIdx.x] = mx;
+    }
+}
+
+template <typename T>
+__global__ void k_minmax_final(const T* __restrict__ pmin, const T* __restrict__ pmax, int nblocks, int d,
+                               T* __restrict__ out /* [2d]: mins, maxs */) {
+    const int k = threadIdx.x;
+    if (k >= d) return;
+    T mn = Elem<T>::highest(), mx = -Elem<T>::highest();
+    for (int b = 0; b < nblocks; ++b) {
+        T a = pmin[(int64_t)b * d + k], c = pmax[(int64_t)b * d + k];
+        if (a < mn) mn = a;
+        if (mx < c) mx = c;
+    }
+    out[k] = mn;
+    out[d + k] = mx;
+}
+
+// ------------------------------------------------------------- cell ids
+struct CellParams {
+    Grid g;
+    double mins_d[kMaxDims];  // per original dimension, stored as double (exact for float/double)
+    double eps;
+    double recip;
+    int cell_mode;
+};
+
+template <typename T, typename K>
+__global__ void k_cell_keys(const T* __restrict__ data, int64_t n, CellParams cp, K* __restrict__ keys,
+                            int32_t* __restrict__ idx) {
+    using F = typename Elem<T>::F;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int d = cp.g.d;
+    const T* p = data + i * d;
+    unsigned long long key = 0;
+    for (int s = 0; s < d; ++s) {
+        const int k = cp.g.swapped[s];
+        key += cell_coord<T>(p[k], (T)cp.mins_d[k], (F)cp.eps, (F)cp.recip, cp.cell_mode) * cp.g.stride[s];
+    }
+    keys[i] = (K)key;
+    idx[i] = (int32_t)i;
+}
+
+// sorted coordinates, one plane per dimension: coords[k * n + i] = data[perm[i] * d + k]
+template <typename T>
+__global__ void k_gather(const T* __restrict__ data, int64_t n, int d, const int32_t* __restrict__ perm,
+                         T* __restrict__ coords) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t src = (int64_t)perm[i] * d;
+    for (int k = 0; k < d; ++k) coords[(int64_t)k * n + i] = data[src + k];
+}
+
+// ------------------------------------------------------------- cell table
+template <typename K>
+__global__ void k_cell_flags(const K* __restrict__ keys, int64_t n, uint32_t* __restrict__ flag) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+// rank[i] = exclusive scan of flags; writes cell start / key and the per-point cell rank
+template <typename K>
+__global__ void k_cell_table(const K* __restrict__ keys, int64_t n, const uint32_t* __restrict__ flag,
+                             uint32_t* __restrict__ rank, int32_t* __restrict__ cell_start,
+                             unsigned long long* __restrict__ cell_key, int32_t* __restrict__ dense) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t f = flag[i];
+    const uint32_t r = rank[i] + f - 1u;  // inclusive rank - 1
+    rank[i] = r;
+    if (f) {
+        cell_start[r] = (int32_t)i;
+        cell_key[r] = (unsigned long long)keys[i];
+        if (dense) dense[(unsigned long long)keys[i]] = (int32_t)r;
+    }
+    if (i == n - 1) cell_start[r + 1] = (int32_t)n;
+}
+
+// Work items of the query kernels: chunks of up to 32 consecutive points of one
+// cell.  item_flag[i] = 1 where a chunk starts.
+static __global__ void k_item_flags(const uint32_t* __restrict__ cellrank, const int32_t* __restrict__ cell_start, int64_t n,
+                             uint32_t* __restrict__ item_flag) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t s = cell_start[cellrank[i]];
+    item_flag[i] = ((i - s) & 31) == 0 ? 1u : 0u;
+}
+
+static __global__ void k_item_write(const uint32_t* __restrict__ item_flag, const uint32_t* __restrict__ item_pos,
+                             const uint32_t* __restrict__ cellrank, int64_t n, int2* __restrict__ items) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (item_flag[i]) items[item_pos[i]] = make_int2((int)cellrank[i], (int)i);
+}
+
+}  // namespace hpd

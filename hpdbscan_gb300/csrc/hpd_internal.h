@@ -1,0 +1,70 @@
+// Internal interfaces between the translation units of the engine.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "hpd_common.cuh"
+
+namespace hpd {
+
+// ------------------------------------------------------------ scan / sort
+int64_t scan_scratch_elems(int64_t n);
+template <typename T>
+void exclusive_scan(const T* in, T* out, int64_t n, T* scratch, T* total, cudaStream_t s, int* launches);
+
+int64_t radix_counts_elems(int64_t n);
+// Sorts (keys, vals) by the low `bits` bits of the keys, stably.  Returns 1 when
+// the result ended up in (keys_alt, vals_alt), 0 when in (keys, vals).
+template <typename K>
+int radix_sort_pairs(K* keys, int32_t* vals, K* keys_alt, int32_t* vals_alt, int64_t n, int bits, uint32_t* counts,
+                     uint32_t* scan_scratch, cudaStream_t s, int* launches);
+
+// ------------------------------------------------------------ device arena
+// Grow-only device buffers owned by one handle: after the first call of a given
+// size no further cudaMalloc happens on that handle.
+struct Arena {
+    void* ptr = nullptr;
+    size_t cap = 0;
+    size_t used = 0;
+    cudaError_t reserve(size_t bytes);
+    void reset() { used = 0; }
+    template <typename T>
+    T* take(size_t count) {
+        size_t off = (used + 255) & ~size_t(255);
+        used = off + count * sizeof(T);
+        return reinterpret_cast<T*>(static_cast<char*>(ptr) + off);
+    }
+    ~Arena();
+};
+
+struct Timers {
+    cudaEvent_t ev[8] = {};
+    bool ok = false;
+};
+
+struct Request {
+    const void* d_data;  // row-major n x d of the element type, device memory
+    int64_t n;
+    int d;
+    float eps;
+    uint64_t min_points;
+    int cell_mode;
+    int dist_mode;
+    int64_t* d_labels;   // device, input order
+    cudaStream_t stream;
+};
+
+struct RunInfo {
+    int64_t n_cells = 0, n_core = 0, n_ambiguous = 0, tie_iterations = 0;
+    int launches = 0;
+    float ms[6] = {0, 0, 0, 0, 0, 0};  // total, index, core, union, border, finalize
+};
+
+// Runs the whole pipeline for element type T.  Returns a Status and fills `err`.
+template <typename T>
+int run_pipeline(const Request& rq, Arena& small, Arena& main, Timers* timers, RunInfo& info, std::string& err);
+
+}  // namespace hpd

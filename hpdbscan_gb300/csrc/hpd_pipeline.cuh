@@ -1,0 +1,313 @@
+// Host orchestration of one clustering call for element type T: every phase runs
+// on the request's stream; the host reads back only the extent (2d values), the
+// cell / work-item counts and the ambiguous-border count.
+#pragma once
+
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "hpd_index.cuh"
+#include "hpd_internal.h"
+#include "hpd_query.cuh"
+
+namespace hpd {
+
+#define HPD_CU(call)                                                              \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) {                                                  \
+            err = std::string(#call) + ": " + cudaGetErrorString(e_);             \
+            return e_ == cudaErrorMemoryAllocation ? kNoMem : kCuda;              \
+        }                                                                         \
+    } while (0)
+
+__global__ void k_iota(int* p, int n);
+
+
+inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// Dispatch over (distance mode, compile-time dimensionality).  For d <= 3 the
+// GCC x86-64 order equals the sequential order.
+#define HPD_QUERY_DISPATCH(KERNEL, T, mode, d, grid, block, smem, stream, args)                                \
+    do {                                                                                                     \
+        if ((d) == 2) {                                                                                      \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 2><<<grid, block, smem, stream>>>(args);       \
+            else KERNEL<T, kDistSeq, 2><<<grid, block, smem, stream>>>(args);                                \
+        } else if ((d) == 3) {                                                                               \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 3><<<grid, block, smem, stream>>>(args);       \
+            else KERNEL<T, kDistSeq, 3><<<grid, block, smem, stream>>>(args);                                \
+        } else {                                                                                             \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 0><<<grid, block, smem, stream>>>(args);       \
+            else if ((mode) == kDistSeq) KERNEL<T, kDistSeq, 0><<<grid, block, smem, stream>>>(args);        \
+            else KERNEL<T, kDistGccX86, 0><<<grid, block, smem, stream>>>(args);                             \
+        }                                                                                                    \
+    } while (0)
+
+template <typename T, typename K>
+int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, std::string& err, const Grid& g,
+                   const T* mins, bool dense_ok);
+
+template <typename T>
+int run_pipeline(const Request& rq, Arena& small, Arena& main, Timers* tm, RunInfo& info, std::string& err) {
+    using F = typename Elem<T>::F;
+    const int64_t n = rq.n;
+    const int d = rq.d;
+    cudaStream_t s = rq.stream;
+    info = RunInfo();
+    if (tm && tm->ok) HPD_CU(cudaEventRecord(tm->ev[0], s));
+
+    // ---- extent (spatial_index.h:99-122)
+    const int64_t count = n * d;
+    const int tpb = (256 / d) * d;
+    int nblk = (int)std::min<int64_t>(1184, (count + tpb - 1) / tpb);
+    if (nblk < 1) nblk = 1;
+    HPD_CU(small.reserve(2 * (size_t)nblk * d * sizeof(T) + 2 * d * sizeof(T) + 1024));
+    small.reset();
+    T* pmin = small.take<T>((size_t)nblk * d);
+    T* pmax = small.take<T>((size_t)nblk * d);
+    T* ext = small.take<T>(2 * d);
+    int* bad = small.take<int>(1);
+    HPD_CU(cudaMemsetAsync(bad, 0, sizeof(int), s));
+    k_minmax_partial<T><<<nblk, tpb, 2 * tpb * sizeof(T), s>>>(static_cast<const T*>(rq.d_data), count, d, pmin, pmax, bad);
+    k_minmax_final<T><<<1, 32, 0, s>>>(pmin, pmax, nblk, d, ext);
+    info.launches += 2;
+    T h_ext[2 * kMaxDims];
+    int h_bad = 0;
+    HPD_CU(cudaMemcpyAsync(h_ext, ext, 2 * d * sizeof(T), cudaMemcpyDeviceToHost, s));
+    HPD_CU(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    HPD_CU(cudaStreamSynchronize(s));
+    if (h_bad) {
+        err = "data contains non-finite coordinates";
+        return kInvalid;
+    }
+
+    // ---- grid geometry (spatial_index.h:124-142), host arithmetic in F
+    Grid g;
+    memset(&g, 0, sizeof g);
+    g.d = d;
+    T mins[kMaxDims];
+    const F epsf = (F)rq.eps;
+    const F recip = (F)1 / epsf;
+    unsigned long long total = 1;
+    for (int k = 0; k < d; ++k) {
+        mins[k] = h_ext[k];
+        const T dmax = h_ext[d + k];
+        const T mx = (Elem<T>::lowest_for_max() < dmax) ? dmax : Elem<T>::lowest_for_max();
+        const F diff = diff_f<T>(mx, mins[k]);
+        const F q = rq.cell_mode == HPD_CELL_RECIP ? diff * recip : diff / epsf;
+        const F c = std::ceil(q);
+        if (!(c >= 0) || c > (F)4.0e18) {
+            err = "cell grid too large in dimension " + std::to_string(k);
+            return kGrid;
+        }
+        g.dims[k] = (unsigned long long)c + 1;
+        if (total > ~0ull / g.dims[k]) {
+            err = "cell grid does not fit 64-bit cell ids";
+            return kGrid;
+        }
+        total *= g.dims[k];
+    }
+    for (int k = 0; k < d; ++k) g.swapped[k] = k;
+    for (int a = 1; a < d; ++a) {  // stable: std::sort on <= 16 elements is an insertion sort
+        int v = g.swapped[a], b = a - 1;
+        while (b >= 0 && g.dims[v] < g.dims[g.swapped[b]]) { g.swapped[b + 1] = g.swapped[b]; --b; }
+        g.swapped[b + 1] = v;
+    }
+    unsigned long long acc = 1;
+    for (int s2 = 0; s2 < d; ++s2) {
+        g.stride[s2] = acc;
+        acc *= g.dims[g.swapped[s2]];
+    }
+    g.total = total;
+    const bool dense_ok = total <= (1ull << 31) && total <= std::max<unsigned long long>(1ull << 26, 8ull * (unsigned long long)n);
+    if (total <= (1ull << 32))
+        return run_pipeline_k<T, uint32_t>(rq, main, tm, info, err, g, mins, dense_ok);
+    return run_pipeline_k<T, unsigned long long>(rq, main, tm, info, err, g, mins, dense_ok);
+}
+
+template <typename T, typename K>
+int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, std::string& err, const Grid& g,
+                   const T* mins, bool dense_ok) {
+    using F = typename Elem<T>::F;
+    const int n = (int)rq.n;
+    const int d = rq.d;
+    cudaStream_t s = rq.stream;
+    const bool timed = tm && tm->ok;
+    int bits = 0;
+    while (bits < 64 && ((g.total - 1) >> bits) != 0) ++bits;
+
+    const int64_t ncounts = radix_counts_elems(n);
+    const int64_t nscan = scan_scratch_elems(std::max<int64_t>(ncounts, n));
+    size_t need = 0;
+    need += 2 * (size_t)n * sizeof(K) + 2 * (size_t)n * 4;          // keys, vals (+ alternates)
+    need += (size_t)n * d * sizeof(T);                               // sorted coordinate planes
+    need += 4 * (size_t)n * 4;                                       // flag, rank, item flag, item pos
+    need += ((size_t)n + 1) * 4 + (size_t)n * 8;                     // cell start, cell key
+    need += dense_ok ? (size_t)g.total * 4 : 0;                      // dense cell lookup
+    need += (size_t)n * 8;                                           // items
+    need += 2 * (size_t)n + 4 * (size_t)n * 4;                       // core, relevant, parent, broot, lm1, amb
+    need += (size_t)ncounts * 4 + (size_t)nscan * 8 + 64;
+    need += 32 * 256;                                                // alignment slack
+    HPD_CU(main.reserve(need));
+    main.reset();
+    K* keys = main.take<K>(n);
+    K* keys_alt = main.take<K>(n);
+    int32_t* vals = main.take<int32_t>(n);
+    int32_t* vals_alt = main.take<int32_t>(n);
+    T* coords = main.take<T>((size_t)n * d);
+    uint32_t* flag = main.take<uint32_t>(n);
+    uint32_t* rank = main.take<uint32_t>(n);
+    uint32_t* iflag = main.take<uint32_t>(n);
+    uint32_t* ipos = main.take<uint32_t>(n);
+    int32_t* cell_start = main.take<int32_t>((size_t)n + 1);
+    unsigned long long* cell_key = main.take<unsigned long long>(n);
+    int32_t* dense = dense_ok ? main.take<int32_t>(g.total) : nullptr;
+    int2* items = main.take<int2>(n);
+    uint8_t* core = main.take<uint8_t>(n);
+    uint8_t* relevant = main.take<uint8_t>(n);
+    int* parent = main.take<int>(n);
+    int* broot = main.take<int>(n);
+    int* lm1 = main.take<int>(n);
+    int* amb = main.take<int>(n);
+    uint32_t* counts = main.take<uint32_t>(ncounts);
+    uint32_t* scan32 = main.take<uint32_t>(2 * nscan);
+    uint32_t* totals = main.take<uint32_t>(4);   // cells, items
+    int* flags_dev = main.take<int>(4);           // n_amb, changed
+
+    // ---- cell ids (spatial_index.h:144-165)
+    CellParams cp;
+    memset(&cp, 0, sizeof cp);
+    cp.g = g;
+    for (int k = 0; k < d; ++k) cp.mins_d[k] = (double)mins[k];
+    cp.eps = (double)(F)rq.eps;
+    cp.recip = (double)((F)1 / (F)rq.eps);
+    cp.cell_mode = rq.cell_mode;
+    const T* data = static_cast<const T*>(rq.d_data);
+    k_cell_keys<T, K><<<blocks_for(n, 256), 256, 0, s>>>(data, n, cp, keys, vals);
+    info.launches += 1;
+
+    // ---- stable sort by cell id (spatial_index.h:184-216)
+    K* skeys = keys;
+    int32_t* perm = vals;
+    if (bits > 0) {
+        const int alt = radix_sort_pairs<K>(keys, vals, keys_alt, vals_alt, n, bits, counts, scan32, s, &info.launches);
+        if (alt) { skeys = keys_alt; perm = vals_alt; }
+    }
+    k_gather<T><<<blocks_for(n, 256), 256, 0, s>>>(data, n, d, perm, coords);
+
+    // ---- cell table (spatial_index.h:167-182) and work items
+    if (dense) HPD_CU(cudaMemsetAsync(dense, 0xff, (size_t)g.total * 4, s));
+    k_cell_flags<K><<<blocks_for(n, 256), 256, 0, s>>>(skeys, n, flag);
+    exclusive_scan<uint32_t>(flag, rank, n, scan32, totals + 0, s, &info.launches);
+    k_cell_table<K><<<blocks_for(n, 256), 256, 0, s>>>(skeys, n, flag, rank, cell_start, cell_key, dense);
+    k_item_flags<<<blocks_for(n, 256), 256, 0, s>>>(rank, cell_start, n, iflag);
+    exclusive_scan<uint32_t>(iflag, ipos, n, scan32, totals + 1, s, &info.launches);
+    k_item_write<<<blocks_for(n, 256), 256, 0, s>>>(iflag, ipos, rank, n, items);
+    info.launches += 5;
+    uint32_t h_tot[2];
+    HPD_CU(cudaMemcpyAsync(h_tot, totals, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    HPD_CU(cudaStreamSynchronize(s));
+    const int m = (int)h_tot[0];
+    const int n_items = (int)h_tot[1];
+    info.n_cells = m;
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[1], s));
+
+    QueryArgs<T> a;
+    memset(&a, 0, sizeof a);
+    a.coords = coords;
+    a.n = n;
+    a.g = g;
+    a.ct.start = cell_start;
+    a.ct.key = cell_key;
+    a.ct.dense = dense;
+    a.ct.m = m;
+    a.eps2 = (T)(rq.eps * rq.eps);  // const float EPS2 = eps * eps (hpdbscan.h:53), converted to T
+    a.items = items;
+    a.n_items = n_items;
+    a.min_points = (int)std::min<uint64_t>(rq.min_points, (uint64_t)n + 1);
+    a.core = core;
+    a.parent = parent;
+    a.broot = broot;
+    a.amb = amb;
+    a.n_amb = flags_dev + 0;
+    a.relevant = relevant;
+    a.lm1 = lm1;
+    a.changed = flags_dev + 1;
+    const int mode = rq.dist_mode;
+    const unsigned qgrid = blocks_for(n_items, 4);
+    const size_t qsmem = 4 * ((size_t)d * 32 * sizeof(T) + 32 * sizeof(int));
+
+    // ---- core test (hpdbscan.h:72-78)
+    if (rq.min_points <= 1) {
+        HPD_CU(cudaMemsetAsync(core, 1, n, s));
+    } else if (rq.min_points > (uint64_t)n) {
+        HPD_CU(cudaMemsetAsync(core, 0, n, s));
+    } else {
+        HPD_QUERY_DISPATCH(k_core, T, mode, d, qgrid, 128, qsmem, s, a);
+        info.launches += 1;
+    }
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[2], s));
+
+    // ---- core-core connectivity
+    k_iota<<<blocks_for(n, 256), 256, 0, s>>>(parent, n);
+    HPD_QUERY_DISPATCH(k_union, T, mode, d, qgrid, 128, qsmem, s, a);
+    k_compress<<<blocks_for(n, 256), 256, 0, s>>>(parent, core, n);
+    info.launches += 3;
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[3], s));
+
+    // ---- borders and the tie-break
+    HPD_CU(cudaMemsetAsync(flags_dev, 0, 4 * sizeof(int), s));
+    HPD_QUERY_DISPATCH(k_border, T, mode, d, qgrid, 128, qsmem, s, a);
+    info.launches += 1;
+    int h_amb = 0;
+    HPD_CU(cudaMemcpyAsync(&h_amb, flags_dev, sizeof(int), cudaMemcpyDeviceToHost, s));
+    HPD_CU(cudaStreamSynchronize(s));
+    info.n_ambiguous = h_amb;
+    if (h_amb > 0) {
+        HPD_CU(cudaMemsetAsync(relevant, 0, n, s));
+        HPD_QUERY_DISPATCH(k_tie_mark, T, mode, d, blocks_for(h_amb, 4), 128, 0, s, a);
+        k_tie_init<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, relevant, lm1, n);
+        info.launches += 2;
+        const int kMaxTieIters = 100000;
+        int it = 0;
+        for (;; ++it) {
+            if (it >= kMaxTieIters) {
+                err = "border tie-break did not converge";
+                return kTimeout;
+            }
+            HPD_CU(cudaMemsetAsync(flags_dev + 1, 0, sizeof(int), s));
+            HPD_QUERY_DISPATCH(k_tie_edge, T, mode, d, qgrid, 128, qsmem, s, a);
+            int h_changed = 0;
+            HPD_CU(cudaMemcpyAsync(&h_changed, flags_dev + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+            HPD_CU(cudaStreamSynchronize(s));
+            info.launches += 1;
+            if (!h_changed) break;
+            k_tie_jump<<<blocks_for(n, 256), 256, 0, s>>>(lm1, n);
+            info.launches += 1;
+        }
+        info.tie_iterations = it + 1;
+        HPD_QUERY_DISPATCH(k_tie_resolve, T, mode, d, blocks_for(h_amb, 4), 128, 0, s, a);
+        info.launches += 1;
+    }
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[4], s));
+
+    // ---- labels in input order
+    k_finalize<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, broot, perm, n, rq.d_labels);
+    info.launches += 1;
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[5], s));
+    HPD_CU(cudaGetLastError());
+    HPD_CU(cudaStreamSynchronize(s));
+    if (timed) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[5]); info.ms[0] = ms;
+        cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[1]); info.ms[1] = ms;
+        cudaEventElapsedTime(&ms, tm->ev[1], tm->ev[2]); info.ms[2] = ms;
+        cudaEventElapsedTime(&ms, tm->ev[2], tm->ev[3]); info.ms[3] = ms;
+        cudaEventElapsedTime(&ms, tm->ev[3], tm->ev[4]); info.ms[4] = ms;
+        cudaEventElapsedTime(&ms, tm->ev[4], tm->ev[5]); info.ms[5] = ms;
+    }
+    return kOk;
+}
+
+}  // namespace hpd

@@ -1,0 +1,110 @@
+/*
+ * hpdbscan_gb300 -- C ABI of the GB300 DBSCAN engine.
+ *
+ * A drop-in for the single-node clustering path of HPDBSCAN: same inputs
+ * (an n x d row-major array of one of ten element types, epsilon, minPoints),
+ * same output (one int64 label per point in input order: 0 noise, -k core point of
+ * cluster k, +k border point of cluster k, k = 1 + the position of the cluster's
+ * first core point in cell-sorted order) and the same errors.  Plain pointers and
+ * sizes only; every entry point returns an hpd_status and leaves a message for
+ * hpd_last_error() on failure.
+ *
+ * Upstream interfaces replaced (paths within the HPDBSCAN project):
+ *   hpd_create / hpd_destroy    HPDBSCAN::HPDBSCAN(float epsilon, size_t min_points)
+ *                               include/hpdbscan.h:288-298
+ *   hpd_cluster                 HPDBSCAN::cluster<T>(T* data, int dim0, int dim1, int threads)
+ *                               include/hpdbscan.h:475-486 (explicit instantiations
+ *                               src/hpdbscan.cpp:19-30), Python cluster(ndarray)
+ *                               swig/hpdbscan.i:27-34
+ *   hpd_cluster_device          the same computation on buffers already in device memory
+ *                               (no upstream counterpart; the host entry point uses it)
+ *   hpd_last_error             the what() of the std::invalid_argument / runtime_error
+ *                               the upstream class throws (hpdbscan.h:296,327,340,350,354)
+ */
+#ifndef HPDBSCAN_GB300_H
+#define HPDBSCAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  HPD_ERR_INVALID corresponds to upstream std::invalid_argument,
+ * HPD_ERR_RUNTIME to std::runtime_error; the others are engine conditions. */
+typedef enum {
+    HPD_OK = 0,
+    HPD_ERR_INVALID = 1,     /* bad epsilon, shape, non-finite coordinate, missing file/dataset */
+    HPD_ERR_UNSUPPORTED = 2, /* unsupported element type / precision / dimensionality */
+    HPD_ERR_RUNTIME = 3,     /* read/write failure */
+    HPD_ERR_GRID = 4,        /* cell grid does not fit 64-bit cell ids */
+    HPD_ERR_NOMEM = 5,       /* device or host allocation failed */
+    HPD_ERR_CUDA = 6,        /* CUDA runtime error */
+    HPD_ERR_TIMEOUT = 7      /* a bounded device loop hit its iteration limit */
+} hpd_status;
+
+/* Element types: the ten upstream instantiations (src/hpdbscan.cpp:19-30). */
+typedef enum {
+    HPD_F32 = 0, HPD_F64 = 1,
+    HPD_I8 = 2, HPD_I16 = 3, HPD_I32 = 4, HPD_I64 = 5,
+    HPD_U8 = 6, HPD_U16 = 7, HPD_U32 = 8, HPD_U64 = 9
+} hpd_dtype;
+
+/* Arithmetic of the reference build being matched.  Upstream computes cell
+ * coordinates as floor((x - min) / eps) (spatial_index.h:156) and squared distances
+ * by a running sum (spatial_index.h:751-754); its CMake flags (-Ofast) let the
+ * compiler turn the division into a multiply by 1/eps and reassociate the sum.
+ * The defaults reproduce GCC -Ofast on x86-64: reciprocal cell coordinates and
+ * the SSE2 partial-sum order. */
+typedef enum { HPD_CELL_RECIP = 0, HPD_CELL_DIV = 1 } hpd_cell_mode;
+typedef enum { HPD_DIST_GCC_X86 = 0, HPD_DIST_SEQ = 1, HPD_DIST_SEQ_FMA = 2 } hpd_dist_mode;
+
+typedef struct hpd_handle hpd_handle;
+
+/* Phase timings of the last call on a handle, in milliseconds of device time. */
+typedef struct {
+    double total_ms;
+    double index_ms;    /* min/max, cell ids, radix sort, gather, cell table */
+    double core_ms;     /* neighbour counts with early exit at minPoints */
+    double union_ms;    /* core-core connectivity */
+    double border_ms;   /* border assignment incl. the tie-break */
+    double finalize_ms; /* labels + un-permute */
+    int64_t n_cells;    /* non-empty cells */
+    int64_t n_core;
+    int64_t n_ambiguous; /* border points adjacent to >= 2 clusters */
+    int64_t tie_iterations;
+    int64_t kernel_launches;
+} hpd_stats;
+
+/* HPDBSCAN(epsilon, min_points): fails with HPD_ERR_INVALID and the upstream
+ * message "epsilon needs to be positive" when epsilon <= 0. */
+int hpd_create(float epsilon, uint64_t min_points, hpd_handle** out);
+void hpd_destroy(hpd_handle* h);
+
+int hpd_set_arith(hpd_handle* h, int cell_mode, int dist_mode);
+
+/* Labels for n points of d coordinates (row-major, host memory) into labels[n]
+ * (host memory), in input order.  `threads` is accepted for interface parity and
+ * unused: the work runs on the current CUDA device. */
+int hpd_cluster(hpd_handle* h, const void* data, int64_t n, int32_t d, int32_t dtype, int32_t threads,
+                int64_t* labels);
+
+/* Same, with data and labels in device memory, ordered on `stream`
+ * (a cudaStream_t; NULL = the handle's own stream).  Returns after the labels
+ * are written (the call synchronises the stream). */
+int hpd_cluster_device(hpd_handle* h, const void* d_data, int64_t n, int32_t d, int32_t dtype,
+                       int64_t* d_labels, void* stream);
+
+int hpd_get_stats(const hpd_handle* h, hpd_stats* out);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* hpd_last_error(void);
+
+/* Version string of the engine. */
+const char* hpd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
