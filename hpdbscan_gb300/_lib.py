@@ -23,7 +23,8 @@ EXPORTS = ("hpd_create", "hpd_destroy", "hpd_set_arith", "hpd_cluster", "hpd_clu
 
 class Stats(ctypes.Structure):
     _fields_ = [("total_ms", ctypes.c_double), ("index_ms", ctypes.c_double), ("core_ms", ctypes.c_double),
-                ("union_ms", ctypes.c_double), ("border_ms", ctypes.c_double), ("finalize_ms", ctypes.c_double),
+                ("union_ms", ctypes.c_double), ("border_ms", ctypes.c_double), ("tie_ms", ctypes.c_double),
+                ("finalize_ms", ctypes.c_double),
                 ("n_cells", ctypes.c_int64), ("n_core", ctypes.c_int64), ("n_ambiguous", ctypes.c_int64),
                 ("tie_iterations", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
 

@@ -169,7 +169,8 @@ int hpd_get_stats(const hpd_handle* h, hpd_stats* out) {
     out->core_ms = h->last.ms[2];
     out->union_ms = h->last.ms[3];
     out->border_ms = h->last.ms[4];
-    out->finalize_ms = h->last.ms[5];
+    out->tie_ms = h->last.ms[5];
+    out->finalize_ms = h->last.ms[6];
     out->n_cells = h->last.n_cells;
     out->n_core = h->last.n_core;
     out->n_ambiguous = h->last.n_ambiguous;

@@ -60,7 +60,7 @@ struct Request {
 struct RunInfo {
     int64_t n_cells = 0, n_core = 0, n_ambiguous = 0, tie_iterations = 0;
     int launches = 0;
-    float ms[6] = {0, 0, 0, 0, 0, 0};  // total, index, core, union, border, finalize
+    float ms[7] = {0, 0, 0, 0, 0, 0, 0};  // total, index, core, union, border, tie-break, finalize
 };
 
 // Runs the whole pipeline for element type T.  Returns a Status and fills `err`.

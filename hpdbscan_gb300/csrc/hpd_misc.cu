@@ -8,6 +8,11 @@ __global__ void k_iota(int* p, int n) {
     if (i < n) p[i] = i;
 }
 
+__global__ void k_fill_int(int* p, int n, int v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
 cudaError_t Arena::reserve(size_t bytes) {
     if (bytes <= cap) return cudaSuccess;
     if (ptr) {

@@ -4,7 +4,10 @@
 #pragma once
 
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <vector>
 #include <string>
 
 #include "hpd_index.cuh"
@@ -23,24 +26,25 @@ namespace hpd {
     } while (0)
 
 __global__ void k_iota(int* p, int n);
+__global__ void k_fill_int(int* p, int n, int v);
 
 
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 // Dispatch over (distance mode, compile-time dimensionality).  For d <= 3 the
 // GCC x86-64 order equals the sequential order.
-#define HPD_QUERY_DISPATCH(KERNEL, T, mode, d, grid, block, smem, stream, args)                                \
+#define HPD_QUERY_DISPATCH(KERNEL, T, mode, d, grid, block, smem, stream, ...)                                 \
     do {                                                                                                     \
         if ((d) == 2) {                                                                                      \
-            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 2><<<grid, block, smem, stream>>>(args);       \
-            else KERNEL<T, kDistSeq, 2><<<grid, block, smem, stream>>>(args);                                \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 2><<<grid, block, smem, stream>>>(__VA_ARGS__);       \
+            else KERNEL<T, kDistSeq, 2><<<grid, block, smem, stream>>>(__VA_ARGS__);                                \
         } else if ((d) == 3) {                                                                               \
-            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 3><<<grid, block, smem, stream>>>(args);       \
-            else KERNEL<T, kDistSeq, 3><<<grid, block, smem, stream>>>(args);                                \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 3><<<grid, block, smem, stream>>>(__VA_ARGS__);       \
+            else KERNEL<T, kDistSeq, 3><<<grid, block, smem, stream>>>(__VA_ARGS__);                                \
         } else {                                                                                             \
-            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 0><<<grid, block, smem, stream>>>(args);       \
-            else if ((mode) == kDistSeq) KERNEL<T, kDistSeq, 0><<<grid, block, smem, stream>>>(args);        \
-            else KERNEL<T, kDistGccX86, 0><<<grid, block, smem, stream>>>(args);                             \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);       \
+            else if ((mode) == kDistSeq) KERNEL<T, kDistSeq, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);        \
+            else KERNEL<T, kDistGccX86, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);                             \
         }                                                                                                    \
     } while (0)
 
@@ -146,7 +150,10 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     need += ((size_t)n + 1) * 4 + (size_t)n * 8;                     // cell start, cell key
     need += dense_ok ? (size_t)g.total * 4 : 0;                      // dense cell lookup
     need += (size_t)n * 8;                                           // items
-    need += 2 * (size_t)n + 4 * (size_t)n * 4;                       // core, relevant, parent, broot, lm1, amb
+    need += (size_t)n + 5 * (size_t)n * 4;                           // core, tmax, parent, broot, lm1, amb
+    need += (size_t)n * 4 + (size_t)n;                               // cell rep, cell flags
+    need += 7 * (size_t)n * 4;                                       // dirty / schedule stamps, dirty list, work lists, cell / item min
+    need += (size_t)n * 4;                                           // second ambiguous list
     need += (size_t)ncounts * 4 + (size_t)nscan * 8 + 64;
     need += 32 * 256;                                                // alignment slack
     HPD_CU(main.reserve(need));
@@ -165,15 +172,25 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     int32_t* dense = dense_ok ? main.take<int32_t>(g.total) : nullptr;
     int2* items = main.take<int2>(n);
     uint8_t* core = main.take<uint8_t>(n);
-    uint8_t* relevant = main.take<uint8_t>(n);
+    int* tmax = main.take<int>(n);
     int* parent = main.take<int>(n);
     int* broot = main.take<int>(n);
     int* lm1 = main.take<int>(n);
     int* amb = main.take<int>(n);
+    int* amb2 = main.take<int>(n);
+    int* cell_rep = main.take<int>(n);
+    uint8_t* cell_flags = main.take<uint8_t>(n);
+    int* dirty_gen = main.take<int>(n);
+    int* sched_gen = main.take<int>(n);
+    int* dlist = main.take<int>(n);
+    int* wl0 = main.take<int>(n);
+    int* wl1 = main.take<int>(n);
+    int* cell_min_l = main.take<int>(n);
+    int* item_min_l = main.take<int>(n);
     uint32_t* counts = main.take<uint32_t>(ncounts);
     uint32_t* scan32 = main.take<uint32_t>(2 * nscan);
     uint32_t* totals = main.take<uint32_t>(4);   // cells, items
-    int* flags_dev = main.take<int>(4);           // n_amb, changed
+    int* flags_dev = main.take<int>(8);           // list counters
 
     // ---- cell ids (spatial_index.h:144-165)
     CellParams cp;
@@ -231,9 +248,12 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     a.broot = broot;
     a.amb = amb;
     a.n_amb = flags_dev + 0;
-    a.relevant = relevant;
+    a.tmax = tmax;
     a.lm1 = lm1;
     a.changed = flags_dev + 1;
+    a.cellrank = rank;
+    a.cell_rep = cell_rep;
+    a.cell_flags = cell_flags;
     const int mode = rq.dist_mode;
     const unsigned qgrid = blocks_for(n_items, 4);
     const size_t qsmem = 4 * ((size_t)d * 32 * sizeof(T) + 32 * sizeof(int));
@@ -251,61 +271,142 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
 
     // ---- core-core connectivity
     k_iota<<<blocks_for(n, 256), 256, 0, s>>>(parent, n);
-    HPD_QUERY_DISPATCH(k_union, T, mode, d, qgrid, 128, qsmem, s, a);
+    HPD_QUERY_DISPATCH(k_union_intra, T, mode, d, qgrid, 128, qsmem, s, a);
+    k_fill_int<<<blocks_for(m, 256), 256, 0, s>>>(cell_rep, m, kNoCore);
+    HPD_CU(cudaMemsetAsync(cell_flags, kCellUniform, m, s));
+    k_cell_rep<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep);
+    k_cell_uniform<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep, cell_flags);
+    HPD_QUERY_DISPATCH(k_union_cross, T, mode, d, qgrid, 128, qsmem, s, a);
     k_compress<<<blocks_for(n, 256), 256, 0, s>>>(parent, core, n);
-    info.launches += 3;
+    info.launches += 7;
     if (timed) HPD_CU(cudaEventRecord(tm->ev[3], s));
 
-    // ---- borders and the tie-break
-    HPD_CU(cudaMemsetAsync(flags_dev, 0, 4 * sizeof(int), s));
+    // ---- borders
+    HPD_CU(cudaMemsetAsync(flags_dev, 0, 8 * sizeof(int), s));
     HPD_QUERY_DISPATCH(k_border, T, mode, d, qgrid, 128, qsmem, s, a);
     info.launches += 1;
     int h_amb = 0;
     HPD_CU(cudaMemcpyAsync(&h_amb, flags_dev, sizeof(int), cudaMemcpyDeviceToHost, s));
     HPD_CU(cudaStreamSynchronize(s));
     info.n_ambiguous = h_amb;
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[4], s));
+
+    // ---- tie-break for borders next to several clusters
     if (h_amb > 0) {
-        HPD_CU(cudaMemsetAsync(relevant, 0, n, s));
-        HPD_QUERY_DISPATCH(k_tie_mark, T, mode, d, blocks_for(h_amb, 4), 128, 0, s, a);
-        k_tie_init<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, relevant, lm1, n);
-        info.launches += 2;
-        const int kMaxTieIters = 100000;
-        int it = 0;
-        for (;; ++it) {
-            if (it >= kMaxTieIters) {
-                err = "border tie-break did not converge";
-                return kTimeout;
-            }
-            HPD_CU(cudaMemsetAsync(flags_dev + 1, 0, sizeof(int), s));
-            HPD_QUERY_DISPATCH(k_tie_edge, T, mode, d, qgrid, 128, qsmem, s, a);
-            int h_changed = 0;
-            HPD_CU(cudaMemcpyAsync(&h_changed, flags_dev + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+        const bool trace = getenv("HPD_TIE_TRACE") != nullptr;
+        k_tie_init<<<blocks_for(n, 256), 256, 0, s>>>(core, lm1, n);
+        HPD_CU(cudaMemsetAsync(dirty_gen, 0, (size_t)m * sizeof(int), s));
+        HPD_CU(cudaMemsetAsync(sched_gen, 0, (size_t)m * sizeof(int), s));
+        info.launches += 1;
+        a.dirty_gen = dirty_gen;
+        a.sched_gen = sched_gen;
+        a.dlist = dlist;
+        a.n_dlist = flags_dev + 1;
+        a.ipos = ipos;
+        a.cell_min_l = cell_min_l;
+        a.item_min_l = item_min_l;
+        a.gen = 0;
+        // ping-pong lists of undecided borders (amb, amb2) and of work items (wl0, wl1)
+        int* lists[2] = {amb, amb2};
+        int* counts[2] = {flags_dev + 0, flags_dev + 2};
+        int* wls[2] = {wl0, wl1};
+        int* wcounts[2] = {flags_dev + 3, flags_dev + 4};
+        int cur = 0, wcur = 0;
+        const int kMaxTiePasses = 1 << 20;
+        const int kPassesPerCheck = 4;
+        const unsigned list_grid = 152 * 8;
+        int h_left = h_amb;
+        // round 0 decides with positions as bounds, round 1 with greedy-descent bounds
+        for (int round = 0; round < 2 && h_left > 0; ++round) {
+            a.amb = lists[cur];
+            a.n_amb = counts[cur];
+            a.amb_out = lists[cur ^ 1];
+            a.n_amb_out = counts[cur ^ 1];
+            HPD_CU(cudaMemsetAsync(a.n_amb_out, 0, sizeof(int), s));
+            HPD_QUERY_DISPATCH(k_tie_decide, T, mode, d, blocks_for(h_left, 4), 128, 0, s, a, 0);
+            cur ^= 1;
+            HPD_CU(cudaMemcpyAsync(&h_left, counts[cur], sizeof(int), cudaMemcpyDeviceToHost, s));
             HPD_CU(cudaStreamSynchronize(s));
             info.launches += 1;
-            if (!h_changed) break;
-            k_tie_jump<<<blocks_for(n, 256), 256, 0, s>>>(lm1, n);
+            if (trace) fprintf(stderr, "[hpd tie] round %d undecided %d\n", round, h_left);
+            if (h_left == 0) break;
+            a.amb = lists[cur];
+            a.n_amb = counts[cur];
+            HPD_CU(cudaMemsetAsync(tmax, 0xff, (size_t)n * sizeof(int), s));
+            HPD_QUERY_DISPATCH(k_tie_mark, T, mode, d, blocks_for(h_left, 4), 128, 0, s, a);
             info.launches += 1;
+            if (round == 0 && d <= 5) {
+                HPD_QUERY_DISPATCH(k_tie_greedy, T, mode, d, qgrid, 128, qsmem, s, a);
+                k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
+                k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
+                info.launches += 3;
+            } else {
+                break;
+            }
         }
-        info.tie_iterations = it + 1;
-        HPD_QUERY_DISPATCH(k_tie_resolve, T, mode, d, blocks_for(h_amb, 4), 128, 0, s, a);
-        info.launches += 1;
+        // relaxation passes until every border is decided or the values are exact
+        if (h_left > 0) {
+            k_fill_int<<<blocks_for(m, 256), 256, 0, s>>>(cell_min_l, m, INT_MAX);
+            k_fill_int<<<blocks_for(n_items, 256), 256, 0, s>>>(item_min_l, n_items, INT_MAX);
+            k_tie_cell_min<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
+            info.launches += 2;
+        }
+        int pass = 0;
+        bool converged = false;
+        while (h_left > 0 && !converged) {
+            for (int k = 0; k < kPassesPerCheck; ++k) {
+                if (pass >= kMaxTiePasses) {
+                    err = "border tie-break did not converge";
+                    return kTimeout;
+                }
+                ++pass;
+                a.gen = pass;
+                a.wlist = wls[wcur];
+                a.n_wlist = wcounts[wcur];
+                a.wlist_out = wls[wcur ^ 1];
+                a.n_wlist_out = wcounts[wcur ^ 1];
+                HPD_CU(cudaMemsetAsync(a.n_dlist, 0, sizeof(int), s));
+                HPD_CU(cudaMemsetAsync(a.n_wlist_out, 0, sizeof(int), s));
+                if (pass == 1) HPD_QUERY_DISPATCH(k_tie_edge, T, mode, d, qgrid, 128, qsmem, s, a);
+                else HPD_QUERY_DISPATCH(k_tie_edge_list, T, mode, d, list_grid, 128, qsmem, s, a);
+                k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
+                k_tie_schedule<T><<<list_grid, 128, 0, s>>>(a);
+                info.launches += 3;
+                wcur ^= 1;
+            }
+            int h_work = 0;
+            HPD_CU(cudaMemcpyAsync(&h_work, wcounts[wcur], sizeof(int), cudaMemcpyDeviceToHost, s));
+            HPD_CU(cudaStreamSynchronize(s));
+            converged = h_work == 0;
+            a.amb = lists[cur];
+            a.n_amb = counts[cur];
+            a.amb_out = lists[cur ^ 1];
+            a.n_amb_out = counts[cur ^ 1];
+            HPD_CU(cudaMemsetAsync(a.n_amb_out, 0, sizeof(int), s));
+            HPD_QUERY_DISPATCH(k_tie_decide, T, mode, d, blocks_for(h_left, 4), 128, 0, s, a, converged ? 1 : 0);
+            cur ^= 1;
+            HPD_CU(cudaMemcpyAsync(&h_left, counts[cur], sizeof(int), cudaMemcpyDeviceToHost, s));
+            HPD_CU(cudaStreamSynchronize(s));
+            info.launches += 1;
+            if (trace) fprintf(stderr, "[hpd tie] pass %d work %d undecided %d\n", pass, h_work, h_left);
+        }
+        info.tie_iterations = pass;
     }
-    if (timed) HPD_CU(cudaEventRecord(tm->ev[4], s));
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[5], s));
 
     // ---- labels in input order
     k_finalize<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, broot, perm, n, rq.d_labels);
     info.launches += 1;
-    if (timed) HPD_CU(cudaEventRecord(tm->ev[5], s));
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[6], s));
     HPD_CU(cudaGetLastError());
     HPD_CU(cudaStreamSynchronize(s));
     if (timed) {
         float ms = 0;
-        cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[5]); info.ms[0] = ms;
-        cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[1]); info.ms[1] = ms;
-        cudaEventElapsedTime(&ms, tm->ev[1], tm->ev[2]); info.ms[2] = ms;
-        cudaEventElapsedTime(&ms, tm->ev[2], tm->ev[3]); info.ms[3] = ms;
-        cudaEventElapsedTime(&ms, tm->ev[3], tm->ev[4]); info.ms[4] = ms;
-        cudaEventElapsedTime(&ms, tm->ev[4], tm->ev[5]); info.ms[5] = ms;
+        cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[6]); info.ms[0] = ms;
+        for (int k = 1; k <= 6; ++k) {
+            cudaEventElapsedTime(&ms, tm->ev[k - 1], tm->ev[k]);
+            info.ms[k] = ms;
+        }
     }
     return kOk;
 }

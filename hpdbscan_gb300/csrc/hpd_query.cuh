@@ -33,12 +33,14 @@ __device__ __forceinline__ int find_cell(const CellTable& ct, unsigned long long
     return (lo < ct.m && ct.key[lo] == key) ? lo : -1;
 }
 
-// Visits the item's own cell first, then the other non-empty cells of the 3^d
-// block around it (only those with a smaller cell id when lower_only), calling
-// fn(cell_rank, is_own) warp-uniformly; fn returns false to stop the visit.
+// Visits the non-empty cells of the 3^d block around cell r (sel: 0 all, 1 only
+// smaller cell ids, 2 only larger cell ids), the item's own cell first (or last
+// when own_last), calling fn(cell_rank, is_own) warp-uniformly; fn returns false
+// to stop the visit.
 template <class Fn>
-__device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct, int r, bool lower_only, Fn&& fn) {
-    if (!fn(r, true)) return;
+__device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct, int r, int sel, Fn&& fn,
+                                              bool own_last = false) {
+    if (!own_last && !fn(r, true)) return;
     const unsigned lane = lane_id();
     const unsigned long long key = ct.key[r];
     unsigned long long coord[kMaxDims];
@@ -62,7 +64,7 @@ __device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct
                     if (coord[s] + 1 >= g.dims[g.swapped[s]]) ok = false; else nk += g.stride[s];
                 }
             }
-            if (ok && (!lower_only || nk < key)) nr = find_cell(ct, nk);
+            if (ok && (sel == 0 || (sel == 1 ? nk < key : nk > key))) nr = find_cell(ct, nk);
         }
         unsigned mask = __ballot_sync(0xffffffffu, nr >= 0);
         while (mask) {
@@ -72,6 +74,7 @@ __device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct
             if (!fn(cr, false)) return;
         }
     }
+    if (own_last) fn(r, true);
 }
 
 // Union-find over sorted point positions; roots are component minima.
@@ -109,9 +112,28 @@ struct QueryArgs {
     int* broot;           // border: root of the assigned cluster, -1 noise
     int* amb;             // ambiguous border points
     int* n_amb;
-    uint8_t* relevant;    // per root: component touches an ambiguous border
+    int* tmax;            // per root: highest position of a core next to an undecided border
+                          // (-1: component not involved); only positions <= tmax matter
     int* lm1;             // tie-break value L - 1 (see k_tie_edge)
     int* changed;
+    const uint32_t* cellrank;  // cell rank of every sorted point
+    int* cell_rep;        // smallest core root of the cell after the in-cell unions, kNoCore if none
+    uint8_t* cell_flags;  // kCellUniform: every core of the cell has root cell_rep
+    // tie-break frontier: a cell is dirty in pass g when a value in it dropped in pass g
+    int* dirty_gen;       // last pass that dirtied the cell
+    int* sched_gen;       // last pass whose work list holds the cell's items
+    int gen;              // current pass
+    int* dlist;           // cells dirtied in the current pass
+    int* n_dlist;
+    const int* wlist;     // work items of the current pass
+    const int* n_wlist;
+    int* wlist_out;       // work items of the next pass
+    int* n_wlist_out;
+    const uint32_t* ipos; // item index of each chunk-start point
+    int* cell_min_l;      // per cell: smallest lm1 among its cores (kept current as values drop)
+    int* item_min_l;      // per work item (32-point chunk): the same, one level finer
+    int* amb_out;         // undecided ambiguous borders after a decision round
+    int* n_amb_out;
 };
 
 // Per-warp tile in shared memory: d planes of 32 coordinates plus one aux word.
@@ -198,17 +220,24 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
         if (active && count < limit && within<T, M, D>(a, q, tile, u)) ++count;
     };
     auto done = [&]() { return __all_sync(0xffffffffu, !active || count >= limit); };
-    visit_stencil(a.g, a.ct, r, false, [&](int cr, bool) {
+    visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
         return !scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
     });
     if (active) a.core[p] = count >= limit ? 1 : 0;
 }
 
 // ---------------------------------------------------- core-core connectivity
-// Every core-core eps edge (q < p) is united; candidates already in the query's
-// component are skipped without a distance test.
+// Every core-core eps edge (q < p) is united.  Pass 1 unites the pairs inside each
+// cell; then every cell gets a summary (the smallest component root among its
+// cores, and whether all its cores share it); pass 2 unites pairs across cells
+// and skips, without loading a single coordinate, a neighbour cell that holds no
+// core or whose cores are already in the query cell's component.  Within a tile,
+// candidates already in the query's component are skipped without a distance test.
+constexpr int kNoCore = INT_MAX;
+constexpr uint8_t kCellUniform = 1;
+
 template <typename T, int M, int D>
-__global__ void __launch_bounds__(128) k_union(QueryArgs<T> a) {
+__global__ void __launch_bounds__(128) k_union_intra(QueryArgs<T> a) {
     const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (item >= a.n_items) return;
     const int2 it = a.items[item];
@@ -230,9 +259,62 @@ __global__ void __launch_bounds__(128) k_union(QueryArgs<T> a) {
         }
     };
     auto never = []() { return false; };
-    visit_stencil(a.g, a.ct, r, true, [&](int cr, bool own) {
-        const int ce = own ? pend : a.ct.start[cr + 1];
-        scan_range(a, tile, a.ct.start[cr], ce, aux_of, pair, never);
+    scan_range(a, tile, a.ct.start[r], pend, aux_of, pair, never);
+}
+
+static __global__ void k_cell_rep(const uint8_t* core, int* parent, const uint32_t* cellrank, int n, int* cell_rep) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && core[i]) atomicMin(cell_rep + cellrank[i], uf_find(parent, i));
+}
+
+static __global__ void k_cell_uniform(const uint8_t* core, int* parent, const uint32_t* cellrank, int n,
+                                      const int* cell_rep, uint8_t* cell_flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && core[i]) {
+        const uint32_t c = cellrank[i];
+        if (uf_find(parent, i) != cell_rep[c]) cell_flags[c] = 0;
+    }
+}
+
+// warp-uniform "same component" test of two cores (lane 0 decides)
+__device__ __forceinline__ bool same_component(int* parent, int x, int y) {
+    int same = 0;
+    if (lane_id() == 0) same = uf_find(parent, x) == uf_find(parent, y);
+    return __shfl_sync(0xffffffffu, same, 0) != 0;
+}
+
+template <typename T, int M, int D>
+__global__ void __launch_bounds__(128) k_union_cross(QueryArgs<T> a) {
+    const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (item >= a.n_items) return;
+    const int2 it = a.items[item];
+    const int r = it.x;
+    const int pend = min(it.y + 32, a.ct.start[r + 1]);
+    const int p = it.y + (int)lane_id();
+    const bool active = p < pend && a.core[p];
+    if (!__any_sync(0xffffffffu, active)) return;
+    const Tile<T> tile = warp_tile<T>(a.g.d);
+    T q[D > 0 ? D : kMaxDims];
+    load_query<T, D>(a, p, active, q);
+    int myroot = active ? uf_find(a.parent, p) : -1;
+    const bool uni_r = (a.cell_flags[r] & kCellUniform) != 0;
+    const int rep_r = a.cell_rep[r];
+    auto aux_of = [&](int j) { return a.core[j] ? uf_find(a.parent, j) : -1; };
+    auto pair = [&](int qi, int u, int rep) {
+        if (!active || rep < 0 || rep == myroot) return;
+        if (within<T, M, D>(a, q, tile, u)) {
+            uf_union(a.parent, p, qi);
+            myroot = uf_find(a.parent, p);
+        }
+    };
+    visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
+        if (own) return true;
+        const int rep_c = a.cell_rep[cr];
+        if (rep_c == kNoCore) return true;
+        const bool both = uni_r && (a.cell_flags[cr] & kCellUniform);
+        if (both && same_component(a.parent, rep_r, rep_c)) return true;
+        auto done = [&]() { return both && same_component(a.parent, rep_r, rep_c); };
+        scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
         return true;
     });
 }
@@ -244,7 +326,8 @@ static __global__ void k_compress(int* parent, const uint8_t* core, int n) {
 
 // ---------------------------------------------------------- border assignment
 // A non-core point with core neighbours of a single component joins it; with
-// several it is recorded as ambiguous for the tie-break.
+// several it is recorded as ambiguous for the tie-break.  Cells without cores,
+// and single-component cells of the component already found, are skipped.
 template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_border(QueryArgs<T> a) {
     const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
@@ -269,7 +352,13 @@ __global__ void __launch_bounds__(128) k_border(QueryArgs<T> a) {
         }
     };
     auto done = [&]() { return __all_sync(0xffffffffu, !active || multi); };
-    visit_stencil(a.g, a.ct, r, false, [&](int cr, bool) {
+    visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
+        const int rep_c = a.cell_rep[cr];
+        if (rep_c == kNoCore) return true;
+        if (a.cell_flags[cr] & kCellUniform) {
+            const int root_c = a.parent[rep_c];
+            if (__all_sync(0xffffffffu, !active || multi || r1 == root_c)) return true;
+        }
         return !scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
     });
     if (active) {
@@ -306,7 +395,7 @@ __device__ __forceinline__ void scan_point(const QueryArgs<T>& a, int p, Hit&& h
         int mid = (lo + hi) >> 1;
         if (a.ct.start[mid] <= p) lo = mid; else hi = mid;
     }
-    visit_stencil(a.g, a.ct, lo, false, [&](int cr, bool) {
+    visit_stencil(a.g, a.ct, lo, 0, [&](int cr, bool) {
         const int ce = a.ct.start[cr + 1];
         for (int j = a.ct.start[cr] + (int)lane; j < ce; j += 32) {
             if (!a.core[j]) continue;
@@ -326,16 +415,191 @@ template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_tie_mark(QueryArgs<T> a) {
     const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (w >= *a.n_amb) return;
-    scan_point<T, M, D>(a, a.amb[w], [&](int j) { a.relevant[a.parent[j]] = 1; });
+    scan_point<T, M, D>(a, a.amb[w], [&](int j) { atomicMax(a.tmax + a.parent[j], j); });
 }
 
-static __global__ void k_tie_init(const uint8_t* core, const int* parent, const uint8_t* relevant, int* lm1, int n) {
+static __global__ void k_tie_init(const uint8_t* core, int* lm1, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) lm1[i] = (core[i] && relevant[parent[i]]) ? i : INT_MAX;
+    if (i < n) lm1[i] = core[i] ? i : INT_MAX;
+}
+
+template <typename T>
+__device__ __forceinline__ void mark_dirty_cell(const QueryArgs<T>& a, int c) {
+    if (atomicMax(a.dirty_gen + c, a.gen) < a.gen) a.dlist[atomicAdd(a.n_dlist, 1)] = c;
+}
+
+// One relaxation pass over decreasing core edges for one work item.  Only
+// candidates in cells dirtied since the previous pass are rescanned: for every
+// other candidate q the query already holds L(p) <= L(q) from an earlier pass.
+// Lower cells are scanned first and the result is published at once; the own
+// cell is then rescanned until no lane of the warp improves, so that chains of
+// improvements inside one chunk settle within this pass.
+template <typename T, int M, int D>
+__device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
+    const int2 it = a.items[item];
+    const int r = it.x;
+    const int pend = min(it.y + 32, a.ct.start[r + 1]);
+    const int p = it.y + (int)lane_id();
+    bool active = p < pend && a.core[p];
+    if (active) active = p <= a.tmax[a.parent[p]];
+    if (!__any_sync(0xffffffffu, active)) return;
+    const Tile<T> tile = warp_tile<T>(a.g.d);
+    T q[D > 0 ? D : kMaxDims];
+    load_query<T, D>(a, p, active, q);
+    const int start_l = active ? ld_volatile(a.lm1 + p) : INT_MAX;
+    int myl = start_l;
+    int published = start_l;
+    const int since = a.gen - 1;
+    auto aux_of = [&](int j) { return a.core[j] ? ld_volatile(a.lm1 + j) : INT_MAX; };
+    auto pair = [&](int qi, int u, int lq) {
+        if (!active || lq >= myl || qi >= p) return;
+        if (within<T, M, D>(a, q, tile, u)) myl = lq;
+    };
+    auto publish = [&]() {
+        const bool better = active && myl < published;
+        if (better) {
+            atomicMin(a.lm1 + p, myl);
+            atomicMin(a.cell_min_l + r, myl);
+            atomicMin(a.item_min_l + item, myl);
+            published = myl;
+        }
+        return better;
+    };
+    auto never = []() { return false; };
+    // tiles are aligned with the 32-point chunks of a cell, so each tile is one work
+    // item; a tile whose smallest value cannot improve any lane is skipped unread
+    auto scan_pruned = [&](int cr, int cs, int ce, int worst) {
+        const int first_item = (int)a.ipos[a.ct.start[cr]];
+        for (int t0 = cs; t0 < ce; t0 += 32) {
+            const int ti = first_item + ((t0 - a.ct.start[cr]) >> 5);
+            if (ld_volatile(a.item_min_l + ti) >= worst) continue;
+            scan_range(a, tile, t0, min(t0 + 32, ce), aux_of, pair, never);
+        }
+    };
+    const bool own_dirty = ld_volatile(a.dirty_gen + r) >= since;
+    visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
+        if (own) {
+            // own cell: the lower chunks once, then the warp's own chunk until no
+            // lane improves (at most one round per lane), publishing every round
+            const bool improved = publish();
+            if (!own_dirty && !__any_sync(0xffffffffu, improved)) return true;
+            {
+                int worst = active ? myl : INT_MIN;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+                scan_pruned(r, a.ct.start[r], it.y, worst);
+            }
+            bool again = true;
+            for (int round = 0; again && round < 33; ++round) {
+                publish();
+                scan_range(a, tile, it.y, pend, aux_of, pair, never);
+                again = __any_sync(0xffffffffu, active && myl < published);
+            }
+            publish();
+            return true;
+        }
+        if (ld_volatile(a.dirty_gen + cr) < since) return true;
+        const int rep_c = a.cell_rep[cr];
+        if (rep_c == kNoCore) return true;
+        if ((a.cell_flags[cr] & kCellUniform) && a.tmax[a.parent[rep_c]] < a.ct.start[cr]) return true;
+        // no core of that cell holds a value below any lane's: nothing to gain
+        int worst = active ? myl : INT_MIN;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+        if (ld_volatile(a.cell_min_l + cr) >= worst) return true;
+        scan_pruned(cr, a.ct.start[cr], a.ct.start[cr + 1], worst);
+        return true;
+    }, /*own_last=*/true);
+    if (__any_sync(0xffffffffu, active && myl < start_l) && lane_id() == 0) mark_dirty_cell(a, r);
 }
 
 template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_tie_edge(QueryArgs<T> a) {
+    const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (item >= a.n_items) return;
+    tie_edge_item<T, M, D>(a, item);
+}
+
+// Same pass over a work list, by a fixed grid of warps.
+template <typename T, int M, int D>
+__global__ void __launch_bounds__(128) k_tie_edge_list(QueryArgs<T> a) {
+    const int nw = gridDim.x * 4;
+    const int cnt = *a.n_wlist;
+    for (int wi = blockIdx.x * 4 + (threadIdx.x >> 5); wi < cnt; wi += nw) tie_edge_item<T, M, D>(a, a.wlist[wi]);
+}
+
+// Pointer jumping: L(p) - 1 is reachable from p, so L(p) may take L(L(p) - 1).
+template <typename T>
+__global__ void k_tie_jump(QueryArgs<T> a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    int l = ld_volatile(a.lm1 + i);
+    if (l == INT_MAX || l == i) return;
+    const int l0 = l;
+    for (;;) {  // strictly decreasing, so at most n steps
+        const int ll = ld_volatile(a.lm1 + l);
+        if (ll >= l) break;
+        l = ll;
+    }
+    if (l < l0) {
+        atomicMin(a.lm1 + i, l);
+        const int c = (int)a.cellrank[i];
+        atomicMin(a.cell_min_l + c, l);
+        const int s0 = a.ct.start[c];
+        atomicMin(a.item_min_l + (int)a.ipos[s0] + ((i - s0) >> 5), l);
+        if (a.gen > 0) mark_dirty_cell(a, c);
+    }
+}
+
+// per-cell minimum of the current values of its cores
+template <typename T>
+__global__ void k_tie_cell_min(QueryArgs<T> a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !a.core[i]) return;
+    const int c = (int)a.cellrank[i];
+    atomicMin(a.cell_min_l + c, a.lm1[i]);
+    const int s0 = a.ct.start[c];
+    atomicMin(a.item_min_l + (int)a.ipos[s0] + ((i - s0) >> 5), a.lm1[i]);
+}
+
+// Next pass's work: the items of every cell whose lower stencil or own cell was
+// dirtied in this pass (each cell once per pass), warp per dirty cell.
+template <typename T>
+__global__ void __launch_bounds__(128) k_tie_schedule(QueryArgs<T> a) {
+    const int nw = gridDim.x * 4;
+    const int cnt = *a.n_dlist;
+    const unsigned lane = lane_id();
+    for (int w = blockIdx.x * 4 + (threadIdx.x >> 5); w < cnt; w += nw) {
+        const int c = a.dlist[w];
+        visit_stencil(a.g, a.ct, c, 2, [&](int cr, bool) {
+            const int rep_c = a.cell_rep[cr];
+            if (rep_c == kNoCore) return true;
+            if ((a.cell_flags[cr] & kCellUniform) && a.tmax[a.parent[rep_c]] < a.ct.start[cr]) return true;
+            int base = -1, nit = 0, first = 0;
+            if (lane == 0 && atomicMax(a.sched_gen + cr, a.gen) < a.gen) {
+                const int s0 = a.ct.start[cr];
+                nit = (a.ct.start[cr + 1] - s0 + 31) >> 5;
+                first = (int)a.ipos[s0];
+                base = atomicAdd(a.n_wlist_out, nit);
+            }
+            base = __shfl_sync(0xffffffffu, base, 0);
+            nit = __shfl_sync(0xffffffffu, nit, 0);
+            first = __shfl_sync(0xffffffffu, first, 0);
+            for (int k = (int)lane; base >= 0 && k < nit; k += 32) a.wlist_out[base + k] = first + k;
+            return true;
+        });
+    }
+}
+
+// Greedy descent step: g(p) = some core eps-neighbour below p (p itself if none).
+// Any decreasing core edge leads to a position reachable from p, so following g
+// from p (pointer jumping) ends at an upper bound of L(p) - 1, equal to the
+// component root whenever the descent reaches it.  To descend fast the lower cell
+// across the most significant dimension (all of whose points lie below the whole
+// slice of p) is tried first, then the other lower cells, then the own cell; each
+// lane stops at its first hit.
+template <typename T, int M, int D>
+__global__ void __launch_bounds__(128) k_tie_greedy(QueryArgs<T> a) {
     const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (item >= a.n_items) return;
     const int2 it = a.items[item];
@@ -343,52 +607,54 @@ __global__ void __launch_bounds__(128) k_tie_edge(QueryArgs<T> a) {
     const int pend = min(it.y + 32, a.ct.start[r + 1]);
     const int p = it.y + (int)lane_id();
     bool active = p < pend && a.core[p];
-    if (active) active = a.relevant[a.parent[p]] != 0;
+    if (active) active = p <= a.tmax[a.parent[p]];
     if (!__any_sync(0xffffffffu, active)) return;
     const Tile<T> tile = warp_tile<T>(a.g.d);
     T q[D > 0 ? D : kMaxDims];
     load_query<T, D>(a, p, active, q);
-    const int start_l = active ? ld_volatile(a.lm1 + p) : INT_MAX;
-    int myl = start_l;
-    auto aux_of = [&](int j) { return a.core[j] ? ld_volatile(a.lm1 + j) : INT_MAX; };
-    auto pair = [&](int qi, int u, int lq) {
-        if (!active || lq >= myl || qi >= p) return;
-        if (within<T, M, D>(a, q, tile, u)) myl = lq;
+    int g = active ? p : INT_MAX;
+    bool found = !active;
+    auto aux_of = [&](int j) { return (int)a.core[j]; };
+    auto pair = [&](int qi, int u, int is_core) {
+        if (found || !is_core || qi >= p) return;
+        if (within<T, M, D>(a, q, tile, u)) { g = qi; found = true; }
     };
-    auto never = []() { return false; };
-    visit_stencil(a.g, a.ct, r, true, [&](int cr, bool own) {
-        const int ce = own ? pend : a.ct.start[cr + 1];
-        scan_range(a, tile, a.ct.start[cr], ce, aux_of, pair, never);
-        return true;
-    });
-    if (active && myl < start_l) {
-        atomicMin(a.lm1 + p, myl);
-        *a.changed = 1;
+    auto done = [&]() { return __all_sync(0xffffffffu, found); };
+    // the lower face across the most significant dimension
+    const int top = a.g.d - 1;
+    const unsigned long long key = a.ct.key[r];
+    int face = -1;
+    if ((key / a.g.stride[top]) % a.g.dims[a.g.swapped[top]] > 0) face = find_cell(a.ct, key - a.g.stride[top]);
+    bool all = false;
+    if (face >= 0 && a.cell_rep[face] != kNoCore)
+        all = scan_range(a, tile, a.ct.start[face], a.ct.start[face + 1], aux_of, pair, done);
+    if (!all) {
+        visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
+            if (own) {
+                scan_range(a, tile, a.ct.start[r], pend, aux_of, pair, done);
+                return true;
+            }
+            if (cr == face || a.cell_rep[cr] == kNoCore) return true;
+            return !scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
+        }, /*own_last=*/true);
     }
+    if (active) a.lm1[p] = g;
 }
 
-static __global__ void k_tie_jump(int* lm1, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int l = ld_volatile(lm1 + i);
-    if (l == INT_MAX || l == i) return;
-    const int l0 = l;
-    for (;;) {  // strictly decreasing, so at most n steps
-        const int ll = ld_volatile(lm1 + l);
-        if (ll >= l) break;
-        l = ll;
-    }
-    if (l < l0) atomicMin(lm1 + i, l);
-}
-
+// Decides the ambiguous borders of the list (a.amb, *a.n_amb) that current bounds
+// settle: lm1[q] is an upper bound of L(q) - 1 and the component root a lower
+// bound, so the component holding the smallest upper bound wins as soon as that
+// bound is below the root of every other adjacent component.  With `final` the
+// values are exact and every border is decided.  Undecided borders are appended to
+// (a.amb_out, *a.n_amb_out).
 template <typename T, int M, int D>
-__global__ void __launch_bounds__(128) k_tie_resolve(QueryArgs<T> a) {
+__global__ void __launch_bounds__(128) k_tie_decide(QueryArgs<T> a, int final_pass) {
     const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (w >= *a.n_amb) return;
     const int b = a.amb[w];
-    unsigned long long best = ~0ull;  // (L - 1) << 32 | root
+    unsigned long long best = ~0ull;  // (upper bound of L - 1) << 32 | root
     scan_point<T, M, D>(a, b, [&](int j) {
-        const unsigned long long v = ((unsigned long long)(unsigned)a.lm1[j] << 32) | (unsigned)a.parent[j];
+        const unsigned long long v = ((unsigned long long)(unsigned)ld_volatile(a.lm1 + j) << 32) | (unsigned)a.parent[j];
         if (v < best) best = v;
     });
 #pragma unroll
@@ -396,7 +662,19 @@ __global__ void __launch_bounds__(128) k_tie_resolve(QueryArgs<T> a) {
         const unsigned long long y = __shfl_xor_sync(0xffffffffu, best, o);
         if (y < best) best = y;
     }
-    if (lane_id() == 0) a.broot[b] = (int)(best & 0xffffffffu);
+    const int root_best = (int)(best & 0xffffffffu);
+    const int ub = (int)(best >> 32);
+    int other = INT_MAX;  // smallest root of the other adjacent components
+    scan_point<T, M, D>(a, b, [&](int j) {
+        const int rj = a.parent[j];
+        if (rj != root_best && rj < other) other = rj;
+    });
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) other = min(other, __shfl_xor_sync(0xffffffffu, other, o));
+    if (lane_id() == 0) {
+        if (final_pass || ub < other) a.broot[b] = root_best;
+        else a.amb_out[atomicAdd(a.n_amb_out, 1)] = b;
+    }
 }
 
 // ------------------------------------------------------------------- labels

@@ -68,7 +68,8 @@ typedef struct {
     double index_ms;    /* min/max, cell ids, radix sort, gather, cell table */
     double core_ms;     /* neighbour counts with early exit at minPoints */
     double union_ms;    /* core-core connectivity */
-    double border_ms;   /* border assignment incl. the tie-break */
+    double border_ms;   /* border assignment */
+    double tie_ms;      /* tie-break for borders next to several clusters */
     double finalize_ms; /* labels + un-permute */
     int64_t n_cells;    /* non-empty cells */
     int64_t n_core;
