@@ -1,0 +1,328 @@
+"""Benchmark: Mpoints/s clustered on the 10M-point 3-D workload (bit-exact labels).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+Workload: 10,000,000 x 3 float32 points, 200 Gaussian blobs (sigma log-U[0.005, 0.03],
+Dirichlet(1) weights) + 5 % uniform noise, eps = 0.005, minPoints = 16, seeded
+synthetic data (the upstream benchmark datasets are not available offline).
+
+One step = one full clustering (grid index, core test, connectivity, borders and
+tie-break, labels in input order).  `value` times steps on device-resident input
+with CUDA events on the engine's stream, flushing L2 (256 MiB write) between steps;
+`e2e` times the host-buffer C-ABI call (pinned input copied in, int64 labels copied
+out) on the same workload.  With --gpus N > 1 (torchrun) every rank clusters its own
+replica of the workload (no data-path collective; the path does not shard) and the
+job value is N x points / the slowest rank's time.
+
+--impl reference times the CPU implementation of the same path on the host cores:
+the upstream build when it exists on this host, else the C restatement run with the
+upstream's parallel structure (OpenMP, all host threads), on a spatial crop of the
+workload that keeps its density.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpoints/s clustered (10M 3-D, bit-exact labels)"
+WORKLOAD = "blobs_10m: 10,000,000 x 3 float32, 200 blobs + 5% noise, eps=0.005, minPoints=16, seed 0"
+PROFILE = os.path.join(ROOT, "profiles", "k_core_blobs10m.txt")
+CROP = 0.10  # CPU sample: spatial crop of the workload (keeps its density)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram read+write bytes per k_core launch from the committed ncu summary, if present."""
+    if not os.path.exists(PROFILE):
+        return None
+    for line in open(PROFILE):
+        if line.startswith("traffic_bytes_per_launch:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def candidate_bytes(points, eps):
+    """Algorithmic bytes of one core-test launch: every non-empty cell streams the
+    coordinates of the points of its 3^d neighbour cells once (4 d bytes each), plus
+    the core flag and the neighbour count of every point (1 + 4 bytes).  Also returns
+    the candidate pairs (query point x candidate).  The cell ids follow the reference's
+    grid (cell side eps, origin at the per-dimension minimum)."""
+    n, d = points.shape
+    mn = points.min(axis=0)
+    recip = np.float32(1.0) / np.float32(eps)
+    idx = np.floor((points - mn) * recip).astype(np.int64)
+    dims = idx.max(axis=0) + 3
+    key = np.zeros(n, np.int64)
+    stride = 1
+    for k in range(d):
+        key += (idx[:, k] + 1) * stride
+        stride *= int(dims[k])
+    uk, cnt = np.unique(key, return_counts=True)
+    total = np.zeros(len(uk), np.int64)
+    offs = [0]
+    stride = 1
+    for k in range(d):
+        offs = [o + s * stride for o in offs for s in (-1, 0, 1)]
+        stride *= int(dims[k])
+    for o in offs:
+        pos = np.searchsorted(uk, uk + o)
+        pos = np.minimum(pos, len(uk) - 1)
+        hit = uk[pos] == uk + o
+        total += np.where(hit, cnt[pos], 0)
+    cand = int((cnt * total).sum())
+    return int(total.sum()) * 4 * d + n * 5, cand
+
+
+class Clock:
+    """nvidia-smi clock samples during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self, device_index):
+        try:
+            lines = [l.split(",") for l in open(self.path) if l.strip()]
+        except OSError:
+            return None
+        rows = [[x.strip() for x in l] for l in lines if len(l) >= 9 and l[0].strip() == str(device_index)]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        busy = sorted(sm)[len(sm) // 2:] if sm else []
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_sample(points, eps, min_points, frac):
+    """A spatial crop of the workload that keeps its density: the slab of the
+    `frac` * n points around the median of the first coordinate."""
+    x = points[:, 0]
+    lo, hi = np.quantile(x, [0.5 - frac / 2, 0.5 + frac / 2])
+    sel = points[(x >= lo) & (x < hi)]
+    return np.ascontiguousarray(sel)
+
+
+def time_cpu(points, eps, min_points, steps):
+    from oracle import pyoracle
+    threads = os.cpu_count() or 1
+    if pyoracle.ref_available():
+        kind, fn = "reference", lambda: pyoracle.ref_cluster(points, eps, min_points, threads=threads)
+    else:
+        kind, fn = "port", lambda: pyoracle.cluster(points, eps, min_points, threads=threads)
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    return kind, threads, ts
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from hpdbscan_gb300 import workloads
+    from oracle import pyoracle
+    pyoracle.build(ref=None)
+    w = workloads.blobs_10m(seed=0)
+    crop = cpu_sample(w.points, w.eps, w.min_points, CROP)
+    kind, threads, ts = time_cpu(crop, w.eps, w.min_points, args.warmup + args.steps)
+    timed = ts[args.warmup:]
+    val = len(crop) * len(timed) / sum(timed) / 1e6
+    sample = f"slab of {len(crop)} points around the median x of the 10M workload ({CROP:.0%}), same eps/minPoints"
+    line = {"metric": METRIC, "value": val, "unit": "Mpoints/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * sum(timed) / len(timed), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": sample}, "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": "Mpoints/s", "cores": threads, "kind": kind, "sample": sample},
+            "e2e": {"value": val, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_engine(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from hpdbscan_gb300 import HPDBSCAN, build, workloads
+    if rank == 0:
+        build.build()
+    if world > 1:
+        torch.distributed.barrier()
+    w = workloads.blobs_10m(seed=0)
+    n, d = w.points.shape
+    h = HPDBSCAN(w.eps, w.min_points)
+    stream = torch.cuda.current_stream()
+    x = torch.from_numpy(w.points).cuda()
+    labels = torch.empty(n, dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        h.cluster_device(x.data_ptr(), n, d, np.float32, labels.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        step()
+    stats0 = h.stats()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clock = Clock(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv") if os.path.isdir(
+        os.path.join(ROOT, "gpurun_out")) else f"/tmp/hpd_clocks_{os.getpid()}.csv")
+    step_ms, core_ms, phases = [], [], []
+    launches = 0
+    with clock:
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            st = h.stats()
+            core_ms.append(st["core_ms"])
+            phases.append(st)
+            launches += int(st["kernel_launches"])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        torch.distributed.barrier()
+    value = world * n * args.steps / (total_ms / 1000) / 1e6
+
+    # end to end through the host-buffer entry point (pinned input, labels back to host)
+    pinned = torch.from_numpy(w.points).pin_memory()
+    host_labels = torch.empty(n, dtype=torch.int64).pin_memory()
+    import ctypes
+    from hpdbscan_gb300 import _lib
+    lib = _lib.load()
+
+    def e2e_step():
+        rc = lib.hpd_cluster(h._h, ctypes.c_void_p(pinned.data_ptr()), n, d, _lib.F32, 0,
+                             ctypes.c_void_p(host_labels.data_ptr()))
+        _lib.raise_for(rc)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_s = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_total = sum(e2e_s)
+    if world > 1:
+        t = torch.tensor([e2e_total], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = world * n * args.steps / e2e_total / 1e6
+    same = bool(torch.equal(host_labels.cuda(), labels))
+
+    if rank != 0:
+        return
+    peak, peak_kind = load_peaks()
+    core_bytes, cand = candidate_bytes(w.points, w.eps)
+    core_avg = sum(core_ms) / len(core_ms)
+    achieved = core_bytes / (core_avg / 1000) / 1e9
+    from oracle import pyoracle
+    pyoracle.build(ref=None)
+    crop = cpu_sample(w.points, w.eps, w.min_points, CROP)
+    kind, threads, ts = time_cpu(crop, w.eps, w.min_points, 2)
+    cpu_val = len(crop) / statistics.median(ts) / 1e6
+    mean = lambda key: sum(p[key] for p in phases) / len(phases)
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_points": n, "dims": d, "eps": w.eps, "min_points": w.min_points,
+                   "parallelism": "replicas" if world > 1 else "single", "l2": "flushed between steps (256 MiB write)",
+                   "labels_match_e2e": same},
+        "e2e": {"value": e2e_value, "unit": "Mpoints/s", "h2d_bytes_per_step": n * d * 4, "d2h_bytes_per_step": n * 8,
+                "ms_per_step": 1000 * e2e_total / args.steps},
+        "roofline": {"bound": "hbm", "kernel": "k_core (neighbour count, early exit at minPoints)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "traffic": profile_traffic(), "algorithmic_bytes": core_bytes, "candidate_pairs": cand,
+                     "avg_launch_ms": core_avg},
+        "phases_ms": {k: round(mean(k + "_ms"), 4) for k in ("index", "core", "union", "border", "tie", "finalize")},
+        "cpu_baseline": {"value": cpu_val, "unit": "Mpoints/s", "cores": threads, "kind": kind,
+                         "sample": f"slab of {len(crop)} points around the median x of the 10M workload "
+                                   f"({CROP:.0%}), median of 2 runs"},
+        "gpu_launches": launches,
+        "clocks": clock.summary(local),
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()
