@@ -151,7 +151,8 @@ __global__ void k_cell_flags(const K* __restrict__ keys, int64_t n, uint32_t* __
 template <typename K>
 __global__ void k_cell_table(const K* __restrict__ keys, int64_t n, const uint32_t* __restrict__ flag,
                              uint32_t* __restrict__ rank, int32_t* __restrict__ cell_start,
-                             unsigned long long* __restrict__ cell_key, int32_t* __restrict__ dense) {
+                             unsigned long long* __restrict__ cell_key, int32_t* __restrict__ dense,
+                             uint32_t* __restrict__ ccoord, Grid g) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t f = flag[i];
@@ -161,6 +162,9 @@ __global__ void k_cell_table(const K* __restrict__ keys, int64_t n, const uint32
         cell_start[r] = (int32_t)i;
         cell_key[r] = (unsigned long long)keys[i];
         if (dense) dense[(unsigned long long)keys[i]] = (int32_t)r;
+        const unsigned long long key = (unsigned long long)keys[i];
+        for (int s = 0; s < g.d; ++s)  // grid coordinate along each swapped dimension
+            ccoord[(size_t)s * n + r] = (uint32_t)((key / g.stride[s]) % g.dims[g.swapped[s]]);
     }
     if (i == n - 1) cell_start[r + 1] = (int32_t)n;
 }

@@ -149,6 +149,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     need += 4 * (size_t)n * 4;                                       // flag, rank, item flag, item pos
     need += ((size_t)n + 1) * 4 + (size_t)n * 8;                     // cell start, cell key
     need += dense_ok ? (size_t)g.total * 4 : 0;                      // dense cell lookup
+    need += (size_t)d * n * 4;                                       // cell grid coordinates
     need += (size_t)n * 8;                                           // items
     need += (size_t)n + 5 * (size_t)n * 4;                           // core, tmax, parent, broot, lm1, amb
     need += (size_t)n * 4 + (size_t)n;                               // cell rep, cell flags
@@ -170,6 +171,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     int32_t* cell_start = main.take<int32_t>((size_t)n + 1);
     unsigned long long* cell_key = main.take<unsigned long long>(n);
     int32_t* dense = dense_ok ? main.take<int32_t>(g.total) : nullptr;
+    uint32_t* ccoord = main.take<uint32_t>((size_t)d * n);
     int2* items = main.take<int2>(n);
     uint8_t* core = main.take<uint8_t>(n);
     int* tmax = main.take<int>(n);
@@ -217,7 +219,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     if (dense) HPD_CU(cudaMemsetAsync(dense, 0xff, (size_t)g.total * 4, s));
     k_cell_flags<K><<<blocks_for(n, 256), 256, 0, s>>>(skeys, n, flag);
     exclusive_scan<uint32_t>(flag, rank, n, scan32, totals + 0, s, &info.launches);
-    k_cell_table<K><<<blocks_for(n, 256), 256, 0, s>>>(skeys, n, flag, rank, cell_start, cell_key, dense);
+    k_cell_table<K><<<blocks_for(n, 256), 256, 0, s>>>(skeys, n, flag, rank, cell_start, cell_key, dense, ccoord, g);
     k_item_flags<<<blocks_for(n, 256), 256, 0, s>>>(rank, cell_start, n, iflag);
     exclusive_scan<uint32_t>(iflag, ipos, n, scan32, totals + 1, s, &info.launches);
     k_item_write<<<blocks_for(n, 256), 256, 0, s>>>(iflag, ipos, rank, n, items);
@@ -239,6 +241,8 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     a.ct.key = cell_key;
     a.ct.dense = dense;
     a.ct.m = m;
+    a.ct.ccoord = ccoord;
+    a.ct.pitch = n;
     a.eps2 = (T)(rq.eps * rq.eps);  // const float EPS2 = eps * eps (hpdbscan.h:53), converted to T
     a.items = items;
     a.n_items = n_items;
@@ -256,7 +260,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     a.cell_flags = cell_flags;
     const int mode = rq.dist_mode;
     const unsigned qgrid = blocks_for(n_items, 4);
-    const size_t qsmem = 4 * ((size_t)d * 32 * sizeof(T) + 32 * sizeof(int));
+    const size_t qsmem = 4 * ((size_t)tile_stride(d) * 32 * sizeof(T) + 32 * sizeof(int));
 
     // ---- core test (hpdbscan.h:72-78)
     if (rq.min_points <= 1) {

@@ -20,7 +20,9 @@ struct CellTable {
     const int32_t* start;              // [m + 1] first sorted position of each cell
     const unsigned long long* key;     // [m] cell id
     const int32_t* dense;              // [grid total] cell rank or -1; nullptr -> binary search
+    const uint32_t* ccoord;            // [d][pitch] grid coordinate of each cell, swapped order
     int m;
+    int pitch;
 };
 
 __device__ __forceinline__ int find_cell(const CellTable& ct, unsigned long long key) {
@@ -44,7 +46,7 @@ __device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct
     const unsigned lane = lane_id();
     const unsigned long long key = ct.key[r];
     unsigned long long coord[kMaxDims];
-    for (int s = 0; s < g.d; ++s) coord[s] = (key / g.stride[s]) % g.dims[g.swapped[s]];
+    for (int s = 0; s < g.d; ++s) coord[s] = ct.ccoord[(size_t)s * ct.pitch + r];
     int S = 1;
     for (int s = 0; s < g.d; ++s) S *= 3;
     const int center = (S - 1) / 2;
@@ -137,9 +139,14 @@ struct QueryArgs {
 };
 
 // Per-warp tile in shared memory: d planes of 32 coordinates plus one aux word.
+// Per-warp tile in shared memory: 32 candidates, each padded to tile_stride(d)
+// coordinates (2 or 4 for d <= 4, so that one vector load fetches a candidate),
+// plus one aux word per candidate.
+__host__ __device__ __forceinline__ int tile_stride(int d) { return d <= 2 ? 2 : (d <= 4 ? 4 : d); }
+
 template <typename T>
 struct Tile {
-    T* c;    // [d][32]
+    T* c;      // [32][tile_stride(d)]
     int* aux;  // [32]
 };
 
@@ -147,11 +154,11 @@ template <typename T>
 __device__ __forceinline__ Tile<T> warp_tile(int d) {
     extern __shared__ __align__(16) unsigned char smem_q[];
     const int w = threadIdx.x >> 5;
-    const size_t per = (size_t)d * 32 * sizeof(T) + 32 * sizeof(int);
+    const size_t per = (size_t)tile_stride(d) * 32 * sizeof(T) + 32 * sizeof(int);
     unsigned char* base = smem_q + per * w;
     Tile<T> t;
     t.c = reinterpret_cast<T*>(base);
-    t.aux = reinterpret_cast<int*>(base + (size_t)d * 32 * sizeof(T));
+    t.aux = reinterpret_cast<int*>(base + (size_t)tile_stride(d) * 32 * sizeof(T));
     return t;
 }
 
@@ -161,11 +168,12 @@ template <typename T, class Aux, class Pair, class Done>
 __device__ __forceinline__ bool scan_range(const QueryArgs<T>& a, const Tile<T>& tile, int cs, int ce, Aux&& aux_of,
                                            Pair&& pair, Done&& done) {
     const int d = a.g.d;
+    const int S = tile_stride(d);
     const unsigned lane = lane_id();
     for (int t0 = cs; t0 < ce; t0 += 32) {
         const int j = t0 + (int)lane;
         if (j < ce) {
-            for (int k = 0; k < d; ++k) tile.c[k * 32 + lane] = a.coords[(size_t)k * a.n + j];
+            for (int k = 0; k < d; ++k) tile.c[lane * S + k] = a.coords[(size_t)k * a.n + j];
             tile.aux[lane] = aux_of(j);
         }
         __syncwarp();
@@ -177,14 +185,43 @@ __device__ __forceinline__ bool scan_range(const QueryArgs<T>& a, const Tile<T>&
     return false;
 }
 
+// candidate u of the tile into c[] (vector loads for d = 2..4)
+template <typename T, int D>
+__device__ __forceinline__ void tile_load(const Tile<T>& tile, int u, int d, T* c) {
+    if (D == 2) {
+        if (sizeof(T) == 4) { const float2 v = reinterpret_cast<const float2*>(tile.c)[u]; c[0] = (T)v.x; c[1] = (T)v.y; }
+        else { const double2 v = reinterpret_cast<const double2*>(tile.c)[u]; c[0] = (T)v.x; c[1] = (T)v.y; }
+    } else if (D == 3 || D == 4) {
+        if (sizeof(T) == 4) {
+            const float4 v = reinterpret_cast<const float4*>(tile.c)[u];
+            c[0] = (T)v.x; c[1] = (T)v.y; c[2] = (T)v.z;
+            if (D == 4) c[3] = (T)v.w;
+        } else {
+            const double2 v0 = reinterpret_cast<const double2*>(tile.c)[2 * u];
+            const double2 v1 = reinterpret_cast<const double2*>(tile.c)[2 * u + 1];
+            c[0] = (T)v0.x; c[1] = (T)v0.y; c[2] = (T)v1.x;
+            if (D == 4) c[3] = (T)v1.y;
+        }
+    } else {
+        const int S = tile_stride(d);
+#pragma unroll
+        for (int k = 0; k < kMaxDims; ++k) {
+            if (k >= d) break;
+            c[k] = tile.c[u * S + k];
+        }
+    }
+}
+
 // squared distance from the lane's query (q[]) to tile slot u, compared with eps2
 template <typename T, int M, int D>
 __device__ __forceinline__ bool within(const QueryArgs<T>& a, const T* q, const Tile<T>& tile, int u) {
+    T c[D > 0 ? (D < 4 ? 4 : D) : kMaxDims];
+    tile_load<T, D>(tile, u, a.g.d, c);
     T t[D > 0 ? D : kMaxDims];
 #pragma unroll
     for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
         if (D == 0 && k >= a.g.d) break;
-        t[k] = sub_(q[k], tile.c[k * 32 + u]);
+        t[k] = sub_(q[k], c[k]);
     }
     return fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
 }
@@ -217,7 +254,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
     const int limit = a.min_points;
     auto aux_of = [](int) { return 0; };
     auto pair = [&](int, int u, int) {
-        if (active && count < limit && within<T, M, D>(a, q, tile, u)) ++count;
+        if (active && within<T, M, D>(a, q, tile, u)) ++count;
     };
     auto done = [&]() { return __all_sync(0xffffffffu, !active || count >= limit); };
     visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
@@ -624,7 +661,7 @@ __global__ void __launch_bounds__(128) k_tie_greedy(QueryArgs<T> a) {
     const int top = a.g.d - 1;
     const unsigned long long key = a.ct.key[r];
     int face = -1;
-    if ((key / a.g.stride[top]) % a.g.dims[a.g.swapped[top]] > 0) face = find_cell(a.ct, key - a.g.stride[top]);
+    if (a.ct.ccoord[(size_t)top * a.ct.pitch + r] > 0) face = find_cell(a.ct, key - a.g.stride[top]);
     bool all = false;
     if (face >= 0 && a.cell_rep[face] != kNoCore)
         all = scan_range(a, tile, a.ct.start[face], a.ct.start[face + 1], aux_of, pair, done);
