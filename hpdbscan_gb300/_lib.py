@@ -18,7 +18,8 @@ CELL_RECIP, CELL_DIV = 0, 1
 DIST_GCC_X86, DIST_SEQ, DIST_SEQ_FMA = 0, 1, 2
 
 EXPORTS = ("hpd_create", "hpd_destroy", "hpd_set_arith", "hpd_cluster", "hpd_cluster_device",
-           "hpd_get_stats", "hpd_last_error", "hpd_version")
+           "hpd_get_stats", "hpd_last_error", "hpd_version", "hpd_cluster_device_noalloc",
+           "hpd_noalloc_last_error")
 
 
 class Stats(ctypes.Structure):
@@ -66,6 +67,12 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.hpd_last_error.restype = ctypes.c_char_p
     lib.hpd_version.argtypes = []
     lib.hpd_version.restype = ctypes.c_char_p
+    lib.hpd_cluster_device_noalloc.argtypes = [ctypes.c_float, ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32,
+                                               ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                               ctypes.c_void_p, ctypes.c_void_p]
+    lib.hpd_cluster_device_noalloc.restype = ctypes.c_int
+    lib.hpd_noalloc_last_error.argtypes = []
+    lib.hpd_noalloc_last_error.restype = ctypes.c_char_p
     _lib = lib
     return lib
 

@@ -29,6 +29,7 @@ struct Arena {
     void* ptr = nullptr;
     size_t cap = 0;
     size_t used = 0;
+    bool fixed = false;  // wraps memory it does not own: never allocates or frees
     cudaError_t reserve(size_t bytes);
     void reset() { used = 0; }
     template <typename T>
@@ -55,6 +56,7 @@ struct Request {
     int dist_mode;
     int64_t* d_labels;   // device, input order
     cudaStream_t stream;
+    bool no_dense = false;  // look cells up by binary search only (no grid-sized table)
 };
 
 struct RunInfo {

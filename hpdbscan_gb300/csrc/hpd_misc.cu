@@ -15,6 +15,7 @@ __global__ void k_fill_int(int* p, int n, int v) {
 
 cudaError_t Arena::reserve(size_t bytes) {
     if (bytes <= cap) return cudaSuccess;
+    if (fixed) return cudaErrorMemoryAllocation;
     if (ptr) {
         cudaError_t e = cudaFree(ptr);
         ptr = nullptr;
@@ -33,7 +34,7 @@ cudaError_t Arena::reserve(size_t bytes) {
 }
 
 Arena::~Arena() {
-    if (ptr) cudaFree(ptr);
+    if (ptr && !fixed) cudaFree(ptr);
 }
 
 }  // namespace hpd

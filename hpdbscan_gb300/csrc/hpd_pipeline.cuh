@@ -124,7 +124,7 @@ int run_pipeline(const Request& rq, Arena& small, Arena& main, Timers* tm, RunIn
         acc *= g.dims[g.swapped[s2]];
     }
     g.total = total;
-    const bool dense_ok = total <= (1ull << 31) && total <= std::max<unsigned long long>(1ull << 26, 8ull * (unsigned long long)n);
+    const bool dense_ok = !rq.no_dense && total <= (1ull << 31) && total <= std::max<unsigned long long>(1ull << 26, 8ull * (unsigned long long)n);
     if (total <= (1ull << 32))
         return run_pipeline_k<T, uint32_t>(rq, main, tm, info, err, g, mins, dense_ok);
     return run_pipeline_k<T, unsigned long long>(rq, main, tm, info, err, g, mins, dense_ok);

@@ -99,6 +99,26 @@ int hpd_cluster_device(hpd_handle* h, const void* d_data, int64_t n, int32_t d, 
 
 int hpd_get_stats(const hpd_handle* h, hpd_stats* out);
 
+/* No counterpart in the reference.  Clustering for callers that cannot call
+ * cudaMalloc (a fixed device-memory budget, a framework that owns all device
+ * allocations): same computation and labels as hpd_cluster_device, but every
+ * intermediate buffer lives in one file-scope device array of 16 MiB that the
+ * library keeps on each GPU that loads it until the process exits.  Nothing is
+ * allocated: no cudaMalloc / cudaFree and no handle.
+ *   - at most 32768 points (any d <= 16, float32 or float64); larger inputs fail with
+ *     HPD_ERR_INVALID;
+ *   - data, labels and stream as for hpd_cluster_device (NULL stream = the legacy
+ *     default stream); returns after the labels are written;
+ *   - the first call on a device looks up the array's device address (a one-time
+ *     set-up per device): make that first call before any stream capture;
+ *   - every call uses the same array, which keeps the last call's contents: calls that
+ *     overlap on the GPU (from two host threads or two streams) race;
+ *   - errors are reported by hpd_noalloc_last_error(). */
+int hpd_cluster_device_noalloc(float epsilon, uint64_t min_points, int32_t cell_mode, int32_t dist_mode,
+                               const void* d_data, int64_t n, int32_t d, int32_t dtype, int64_t* d_labels,
+                               void* stream);
+const char* hpd_noalloc_last_error(void);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* hpd_last_error(void);
 
