@@ -1,0 +1,42 @@
+// Test driver for include/hpdbscan.h, written the way an upstream user calls the
+// HPDBSCAN class:  cluster_demo <points.f32> <n> <d> <eps> <minPts> <labels.i64>
+//                  cluster_demo --bad-eps
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <iostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "hpdbscan.h"
+
+int main(int argc, char** argv) {
+    if (argc == 2 && std::string(argv[1]) == "--bad-eps") {
+        try {
+            HPDBSCAN h(-1.0f, 5);
+        } catch (const std::invalid_argument& e) {
+            std::cout << "invalid_argument: " << e.what() << std::endl;
+            return 0;
+        }
+        return 1;
+    }
+    if (argc != 7) return 2;
+    const int n = std::atoi(argv[2]), d = std::atoi(argv[3]);
+    std::vector<float> pts(static_cast<size_t>(n) * d);
+    std::FILE* f = std::fopen(argv[1], "rb");
+    if (!f || std::fread(pts.data(), sizeof(float), pts.size(), f) != pts.size()) return 3;
+    std::fclose(f);
+    HPDBSCAN h(static_cast<float>(std::atof(argv[4])), static_cast<size_t>(std::atol(argv[5])));
+    Clusters c = h.cluster(pts.data(), n, d);
+    std::FILE* o = std::fopen(argv[6], "wb");
+    std::vector<int64_t> out(c.begin(), c.end());
+    std::fwrite(out.data(), sizeof(int64_t), out.size(), o);
+    std::fclose(o);
+    try {
+        h.cluster(std::string("/nonexistent/data.h5"), std::string("DATA"));
+    } catch (const std::invalid_argument& e) {
+        std::cout << "file: " << e.what() << std::endl;
+    }
+    return 0;
+}
