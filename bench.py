@@ -163,6 +163,76 @@ def time_cpu(points, eps, min_points, steps):
     return kind, threads, ts
 
 
+def measure_batched(n_inst, workers):
+    """Batch workload (instances log-U[1e3, 1e6] points, d 2..5, per-instance eps and
+    minPoints): jobs/s of one hpd_cluster_batch call vs the plain per-instance path
+    (one HPDBSCAN object and cluster call per instance), host buffers both ways."""
+    from hpdbscan_gb300 import HPDBSCAN, workloads
+    from hpdbscan_gb300.serve import cluster_batch
+    items = []
+    for i in range(n_inst):
+        w = workloads.batch_instance(i)
+        items.append((w.points, w.eps, w.min_points))
+    pts_total = sum(len(it[0]) for it in items)
+    cluster_batch(items[:16], workers=workers)  # warm-up
+    t0 = time.perf_counter()
+    got = cluster_batch(items, workers=workers)
+    tb = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    same = True
+    for it, g in zip(items, got):
+        same &= bool(np.array_equal(HPDBSCAN(it[1], it[2]).cluster_array(it[0]), g))
+    tp = time.perf_counter() - t0
+    return {"instances": n_inst, "points": pts_total, "workers": workers, "jobs_per_s": n_inst / tb,
+            "plain_jobs_per_s": n_inst / tp, "speedup_vs_plain": tp / tb, "mpoints_per_s": pts_total / tb / 1e6,
+            "labels_identical_to_plain": same}
+
+
+def measure_served(duration_s, workers, rate=200.0):
+    """Serving workload: Poisson arrivals (rate/s), n log-U[1e4, 5e6], d in {2,3,4},
+    eps U[0.002, 0.02], minPoints in {8,16,32}; each job's points are the first n of a
+    seeded 5M-point blob mixture of its dimension.  Reports latency percentiles
+    (submission to labels on the host) and jobs/s for the continuous-batching server
+    and for the same trace served one job at a time (1 worker)."""
+    from hpdbscan_gb300 import workloads
+    from hpdbscan_gb300.serve import Server
+    trace = workloads.serve_trace(seed=0, rate=rate, duration_s=duration_s)
+    pools = {}
+    for d in (2, 3, 4):
+        w = workloads.batch_instance(7000 + d, n_max=5_000_001)
+        rng = np.random.default_rng(d)
+        centres = rng.random((40, d))
+        pools[d] = workloads._mixture(rng, 5_000_000, d, centres, np.exp(rng.uniform(np.log(0.005), np.log(0.05), 40)),
+                                      rng.dirichlet(np.ones(40)), 0.05)
+    jobs = [(pools[j.d][:j.n], j.eps, j.min_points, j.arrival_s) for j in trace]
+
+    def replay(n_workers):
+        lat = []
+        with Server(workers=n_workers, budget_bytes=120 << 30, reserve_points=5_000_000, reserve_dims=4) as srv:
+            srv.wait(srv.submit(*jobs[0][:3]))  # warm-up
+            t_start = time.perf_counter()
+            tickets = []
+            for pts, eps, mp, at in jobs:
+                delay = at - (time.perf_counter() - t_start)
+                if delay > 0:
+                    time.sleep(delay)
+                tickets.append(srv.submit(pts, eps, mp))
+            for t in tickets:
+                _, q, r = srv.wait(t, with_stats=True)
+                lat.append(q + r)
+            span = time.perf_counter() - t_start
+        lat = np.array(lat)
+        return {"jobs": len(jobs), "jobs_per_s": len(jobs) / span, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "makespan_s": span}
+
+    served = replay(workers)
+    plain = replay(1)
+    return {"trace": f"Poisson {rate:.0f}/s for {duration_s:.0f} s ({len(jobs)} jobs, "
+                     f"{sum(len(j[0]) for j in jobs) / 1e6:.0f}M points)",
+            "workers": workers, "hbm_budget_gb": 120, **served,
+            "plain": {k: plain[k] for k in ("jobs_per_s", "p50_ms", "p99_ms", "makespan_s")}}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -284,6 +354,8 @@ def run_engine(args):
     kind, threads, ts = time_cpu(crop, w.eps, w.min_points, 2)
     cpu_val = len(crop) / statistics.median(ts) / 1e6
     mean = lambda key: sum(p[key] for p in phases) / len(phases)
+    batched = measure_batched(args.batch_instances, 8) if args.batch_instances > 0 else None
+    served = measure_served(args.serve_seconds, 8) if args.serve_seconds > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -302,6 +374,8 @@ def run_engine(args):
         "cpu_baseline": {"value": cpu_val, "unit": "Mpoints/s", "cores": threads, "kind": kind,
                          "sample": f"slab of {len(crop)} points around the median x of the 10M workload "
                                    f"({CROP:.0%}), median of 2 runs"},
+        "batched": batched,
+        "served": served,
         "gpu_launches": launches,
         "clocks": clock.summary(local),
         "wall_s": wall,
@@ -317,6 +391,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--batch-instances", type=int, default=256, help="batch workload instances (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=4.0, help="length of the serving trace (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

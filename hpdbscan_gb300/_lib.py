@@ -19,7 +19,16 @@ DIST_GCC_X86, DIST_SEQ, DIST_SEQ_FMA = 0, 1, 2
 
 EXPORTS = ("hpd_create", "hpd_destroy", "hpd_set_arith", "hpd_cluster", "hpd_cluster_device",
            "hpd_get_stats", "hpd_last_error", "hpd_version", "hpd_cluster_device_noalloc",
-           "hpd_noalloc_last_error")
+           "hpd_noalloc_last_error", "hpd_cluster_batch", "hpd_server_create", "hpd_server_submit",
+           "hpd_server_poll", "hpd_server_wait", "hpd_server_destroy", "hpd_server_last_error")
+
+
+class Job(ctypes.Structure):
+    """hpd_job of include/hpdbscan_gb300.h."""
+    _fields_ = [("data", ctypes.c_void_p), ("n", ctypes.c_int64), ("d", ctypes.c_int32), ("dtype", ctypes.c_int32),
+                ("epsilon", ctypes.c_float), ("min_points", ctypes.c_uint64), ("cell_mode", ctypes.c_int32),
+                ("dist_mode", ctypes.c_int32), ("labels", ctypes.c_void_p), ("status", ctypes.c_int32),
+                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -73,6 +82,21 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.hpd_cluster_device_noalloc.restype = ctypes.c_int
     lib.hpd_noalloc_last_error.argtypes = []
     lib.hpd_noalloc_last_error.restype = ctypes.c_char_p
+    lib.hpd_cluster_batch.argtypes = [ctypes.POINTER(Job), ctypes.c_int64, ctypes.c_int32]
+    lib.hpd_cluster_batch.restype = ctypes.c_int
+    lib.hpd_server_create.argtypes = [ctypes.c_int32, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int32,
+                                      ctypes.POINTER(H)]
+    lib.hpd_server_create.restype = ctypes.c_int
+    lib.hpd_server_submit.argtypes = [H, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_int64)]
+    lib.hpd_server_submit.restype = ctypes.c_int
+    lib.hpd_server_poll.argtypes = [H, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]
+    lib.hpd_server_poll.restype = ctypes.c_int
+    lib.hpd_server_wait.argtypes = [H, ctypes.c_int64]
+    lib.hpd_server_wait.restype = ctypes.c_int
+    lib.hpd_server_destroy.argtypes = [H]
+    lib.hpd_server_destroy.restype = None
+    lib.hpd_server_last_error.argtypes = []
+    lib.hpd_server_last_error.restype = ctypes.c_char_p
     _lib = lib
     return lib
 

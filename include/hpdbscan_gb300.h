@@ -99,6 +99,47 @@ int hpd_cluster_device(hpd_handle* h, const void* d_data, int64_t n, int32_t d, 
 
 int hpd_get_stats(const hpd_handle* h, hpd_stats* out);
 
+/* ------------------------------------------------------------ batches, serving
+ * No counterpart in the reference (its jobs run one at a time): many independent
+ * clustering jobs on one GPU.  A job names host buffers; it stays owned by the caller
+ * and must stay valid until the job completes. */
+typedef struct {
+    const void* data;      /* host, n x d row-major */
+    int64_t n;
+    int32_t d;
+    int32_t dtype;         /* HPD_F32 or HPD_F64 */
+    float epsilon;
+    uint64_t min_points;
+    int32_t cell_mode;     /* hpd_cell_mode, 0 = default */
+    int32_t dist_mode;     /* hpd_dist_mode, 0 = default */
+    int64_t* labels;       /* host, n: written in input order */
+    int32_t status;        /* out: hpd_status of the job, -1 while pending */
+    double queue_ms;       /* out: submission to start */
+    double run_ms;         /* out: start to labels on the host */
+} hpd_job;
+
+/* Runs every job of the array on the current GPU with n_workers concurrent streams
+ * (0 = 8), largest jobs first.  Returns HPD_OK when all jobs succeeded; each job's own
+ * status is in jobs[i].status. */
+int hpd_cluster_batch(hpd_job* jobs, int64_t n_jobs, int32_t n_workers);
+
+/* A serving loop on the current GPU: n_workers threads, each with its own CUDA stream
+ * and device buffers (sized up front for reserve_points points of reserve_dims
+ * dimensions), take submitted jobs in arrival order; a job is admitted when the device
+ * bytes of the jobs in flight plus its own stay within hbm_budget_bytes (a job is
+ * always admitted onto an idle server), and starts as soon as a worker is free, so jobs
+ * that arrive while others run overlap with them on the device. */
+typedef struct hpd_server hpd_server;
+int hpd_server_create(int32_t n_workers, uint64_t hbm_budget_bytes, int64_t reserve_points, int32_t reserve_dims,
+                      hpd_server** out);
+int hpd_server_submit(hpd_server* s, hpd_job* job, int64_t* ticket);
+int hpd_server_poll(hpd_server* s, int64_t ticket, int32_t* done);
+/* Blocks until the job is done, forgets the ticket and returns the job's status. */
+int hpd_server_wait(hpd_server* s, int64_t ticket);
+/* Finishes the jobs already submitted, then stops the workers. */
+void hpd_server_destroy(hpd_server* s);
+const char* hpd_server_last_error(void);
+
 /* No counterpart in the reference.  Clustering for callers that cannot call
  * cudaMalloc (a fixed device-memory budget, a framework that owns all device
  * allocations): same computation and labels as hpd_cluster_device, but every
