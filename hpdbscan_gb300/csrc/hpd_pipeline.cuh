@@ -153,7 +153,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     need += (size_t)n * 8;                                           // items
     need += (size_t)n + 5 * (size_t)n * 4;                           // core, tmax, parent, broot, lm1, amb
     need += (size_t)n * 4 + (size_t)n;                               // cell rep, cell flags
-    need += 7 * (size_t)n * 4;                                       // dirty / schedule stamps, dirty list, work lists, cell / item min
+    need += 9 * (size_t)n * 4;                                       // dirty / schedule stamps, dirty list, work lists, cell / item min, item flags
     need += (size_t)n * 4;                                           // second ambiguous list
     need += (size_t)ncounts * 4 + (size_t)nscan * 8 + 64;
     need += 32 * 256;                                                // alignment slack
@@ -189,10 +189,12 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     int* wl1 = main.take<int>(n);
     int* cell_min_l = main.take<int>(n);
     int* item_min_l = main.take<int>(n);
+    uint32_t* item_flag = main.take<uint32_t>(n);
+    uint32_t* item_pos = main.take<uint32_t>(n);
     uint32_t* counts = main.take<uint32_t>(ncounts);
     uint32_t* scan32 = main.take<uint32_t>(2 * nscan);
     uint32_t* totals = main.take<uint32_t>(4);   // cells, items
-    int* flags_dev = main.take<int>(8);           // list counters
+    int* flags_dev = main.take<int>(16);          // list counters, diagnostics
 
     // ---- cell ids (spatial_index.h:144-165)
     CellParams cp;
@@ -298,6 +300,8 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     // ---- tie-break for borders next to several clusters
     if (h_amb > 0) {
         const bool trace = getenv("HPD_TIE_TRACE") != nullptr;
+        unsigned long long* tcount = reinterpret_cast<unsigned long long*>(flags_dev + 8);
+        a.trace_counts = trace ? tcount : nullptr;
         k_tie_init<<<blocks_for(n, 256), 256, 0, s>>>(core, lm1, n);
         HPD_CU(cudaMemsetAsync(dirty_gen, 0, (size_t)m * sizeof(int), s));
         HPD_CU(cudaMemsetAsync(sched_gen, 0, (size_t)m * sizeof(int), s));
@@ -309,6 +313,9 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         a.ipos = ipos;
         a.cell_min_l = cell_min_l;
         a.item_min_l = item_min_l;
+        a.item_flag = item_flag;
+        a.ticket = flags_dev + 5;
+        HPD_CU(cudaMemsetAsync(item_flag, 0, (size_t)n_items * sizeof(uint32_t), s));
         a.gen = 0;
         // ping-pong lists of undecided borders (amb, amb2) and of work items (wl0, wl1)
         int* lists[2] = {amb, amb2};
@@ -318,7 +325,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         int cur = 0, wcur = 0;
         const int kMaxTiePasses = 1 << 20;
         const int kPassesPerCheck = 4;
-        const unsigned list_grid = 152 * 8;
+        const unsigned list_grid = 152 * 16;
         int h_left = h_amb;
         // round 0 decides with positions as bounds, round 1 with greedy-descent bounds
         for (int round = 0; round < 2 && h_left > 0; ++round) {
@@ -370,12 +377,24 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 a.wlist_out = wls[wcur ^ 1];
                 a.n_wlist_out = wcounts[wcur ^ 1];
                 HPD_CU(cudaMemsetAsync(a.n_dlist, 0, sizeof(int), s));
-                HPD_CU(cudaMemsetAsync(a.n_wlist_out, 0, sizeof(int), s));
+                HPD_CU(cudaMemsetAsync(a.ticket, 0, sizeof(int), s));
+                if (trace) HPD_CU(cudaMemsetAsync(tcount, 0, 2 * sizeof(unsigned long long), s));
                 if (pass == 1) HPD_QUERY_DISPATCH(k_tie_edge, T, mode, d, qgrid, 128, qsmem, s, a);
                 else HPD_QUERY_DISPATCH(k_tie_edge_list, T, mode, d, list_grid, 128, qsmem, s, a);
                 k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
                 k_tie_schedule<T><<<list_grid, 128, 0, s>>>(a);
-                info.launches += 3;
+                exclusive_scan<uint32_t>(item_flag, item_pos, n_items, scan32,
+                                         reinterpret_cast<uint32_t*>(a.n_wlist_out), s, &info.launches);
+                k_tie_compact<<<blocks_for(n_items, 256), 256, 0, s>>>(item_flag, item_pos, n_items, a.wlist_out);
+                info.launches += 4;
+                if (trace) {
+                    unsigned long long tc[2];
+                    int wn = 0;
+                    cudaMemcpy(tc, tcount, sizeof tc, cudaMemcpyDeviceToHost);
+                    cudaMemcpy(&wn, a.n_wlist, sizeof(int), cudaMemcpyDeviceToHost);
+                    fprintf(stderr, "[hpd tie] pass %d items %d active lanes %llu tiles %llu\n", pass,
+                            pass == 1 ? n_items : wn, tc[0], tc[1]);
+                }
                 wcur ^= 1;
             }
             int h_work = 0;

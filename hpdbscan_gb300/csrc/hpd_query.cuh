@@ -39,9 +39,13 @@ __device__ __forceinline__ int find_cell(const CellTable& ct, unsigned long long
 // smaller cell ids, 2 only larger cell ids), the item's own cell first (or last
 // when own_last), calling fn(cell_rank, is_own) warp-uniformly; fn returns false
 // to stop the visit.
-template <class Fn>
+struct KeepAll {
+    __device__ __forceinline__ bool operator()(int) const { return true; }
+};
+
+template <class Fn, class Keep = KeepAll>
 __device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct, int r, int sel, Fn&& fn,
-                                              bool own_last = false) {
+                                              bool own_last = false, Keep keep = Keep()) {
     if (!own_last && !fn(r, true)) return;
     const unsigned lane = lane_id();
     const unsigned long long key = ct.key[r];
@@ -67,6 +71,8 @@ __device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct
                 }
             }
             if (ok && (sel == 0 || (sel == 1 ? nk < key : nk > key))) nr = find_cell(ct, nk);
+            // the per-cell filter runs on all lanes at once, hiding its load latency
+            if (nr >= 0 && !keep(nr)) nr = -1;
         }
         unsigned mask = __ballot_sync(0xffffffffu, nr >= 0);
         while (mask) {
@@ -134,6 +140,9 @@ struct QueryArgs {
     const uint32_t* ipos; // item index of each chunk-start point
     int* cell_min_l;      // per cell: smallest lm1 among its cores (kept current as values drop)
     int* item_min_l;      // per work item (32-point chunk): the same, one level finer
+    uint32_t* item_flag;  // items scheduled for the next pass
+    int* ticket;          // next work-list entry to take
+    unsigned long long* trace_counts;  // diagnostics (nullptr: off): [0] active lanes, [1] tiles scanned
     int* amb_out;         // undecided ambiguous borders after a decision round
     int* n_amb_out;
 };
@@ -353,7 +362,7 @@ __global__ void __launch_bounds__(128) k_union_cross(QueryArgs<T> a) {
         auto done = [&]() { return both && same_component(a.parent, rep_r, rep_c); };
         scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
         return true;
-    });
+    }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore; });
 }
 
 static __global__ void k_compress(int* parent, const uint8_t* core, int n) {
@@ -397,7 +406,7 @@ __global__ void __launch_bounds__(128) k_border(QueryArgs<T> a) {
             if (__all_sync(0xffffffffu, !active || multi || r1 == root_c)) return true;
         }
         return !scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
-    });
+    }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore; });
     if (active) {
         a.broot[p] = r1;
         if (multi) a.amb[atomicAdd(a.n_amb, 1)] = p;
@@ -478,8 +487,14 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
     const int pend = min(it.y + 32, a.ct.start[r + 1]);
     const int p = it.y + (int)lane_id();
     bool active = p < pend && a.core[p];
-    if (active) active = p <= a.tmax[a.parent[p]];
+    const int root = active ? a.parent[p] : INT_MIN;
+    // a core whose value is its component root holds the smallest value possible
+    if (active) active = p <= a.tmax[root] && ld_volatile(a.lm1 + p) > root;
     if (!__any_sync(0xffffffffu, active)) return;
+    if (a.trace_counts) {
+        const unsigned am = __ballot_sync(0xffffffffu, active);  // every lane takes part
+        if (lane_id() == 0) atomicAdd(a.trace_counts, (unsigned long long)__popc(am));
+    }
     const Tile<T> tile = warp_tile<T>(a.g.d);
     T q[D > 0 ? D : kMaxDims];
     load_query<T, D>(a, p, active, q);
@@ -503,6 +518,8 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
         return better;
     };
     auto never = []() { return false; };
+    // a lane is finished once its value is its component root
+    auto settled = [&]() { return __all_sync(0xffffffffu, !active || myl <= root); };
     // tiles are aligned with the 32-point chunks of a cell, so each tile is one work
     // item; a tile whose smallest value cannot improve any lane is skipped unread
     auto scan_pruned = [&](int cr, int cs, int ce, int worst) {
@@ -510,23 +527,28 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
         for (int t0 = cs; t0 < ce; t0 += 32) {
             const int ti = first_item + ((t0 - a.ct.start[cr]) >> 5);
             if (ld_volatile(a.item_min_l + ti) >= worst) continue;
-            scan_range(a, tile, t0, min(t0 + 32, ce), aux_of, pair, never);
+            if (a.trace_counts && lane_id() == 0) atomicAdd(a.trace_counts + 1, 1ull);
+            if (scan_range(a, tile, t0, min(t0 + 32, ce), aux_of, pair, settled)) return true;
         }
+        return false;
     };
     const bool own_dirty = ld_volatile(a.dirty_gen + r) >= since;
+    int worst0 = active ? myl : INT_MIN;  // largest lane value at the start: a cell must beat it
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) worst0 = max(worst0, __shfl_xor_sync(0xffffffffu, worst0, o));
     visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
         if (own) {
             // own cell: the lower chunks once, then the warp's own chunk until no
             // lane improves (at most one round per lane), publishing every round
             const bool improved = publish();
             if (!own_dirty && !__any_sync(0xffffffffu, improved)) return true;
-            {
-                int worst = active ? myl : INT_MIN;
+            if (!settled()) {
+                int worst = (active && myl > root) ? myl : INT_MIN;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
                 scan_pruned(r, a.ct.start[r], it.y, worst);
             }
-            bool again = true;
+            bool again = !settled();
             for (int round = 0; again && round < 33; ++round) {
                 publish();
                 scan_range(a, tile, it.y, pend, aux_of, pair, never);
@@ -540,13 +562,20 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
         if (rep_c == kNoCore) return true;
         if ((a.cell_flags[cr] & kCellUniform) && a.tmax[a.parent[rep_c]] < a.ct.start[cr]) return true;
         // no core of that cell holds a value below any lane's: nothing to gain
-        int worst = active ? myl : INT_MIN;
+        if (settled()) return true;
+        int worst = (active && myl > root) ? myl : INT_MIN;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
         if (ld_volatile(a.cell_min_l + cr) >= worst) return true;
         scan_pruned(cr, a.ct.start[cr], a.ct.start[cr + 1], worst);
         return true;
-    }, /*own_last=*/true);
+    }, /*own_last=*/true, [&](int cr) {
+        if (ld_volatile(a.dirty_gen + cr) < since) return false;
+        const int rep_c = a.cell_rep[cr];
+        if (rep_c == kNoCore) return false;
+        if ((a.cell_flags[cr] & kCellUniform) && a.tmax[a.parent[rep_c]] < a.ct.start[cr]) return false;
+        return ld_volatile(a.cell_min_l + cr) < worst0;
+    });
     if (__any_sync(0xffffffffu, active && myl < start_l) && lane_id() == 0) mark_dirty_cell(a, r);
 }
 
@@ -557,12 +586,18 @@ __global__ void __launch_bounds__(128) k_tie_edge(QueryArgs<T> a) {
     tie_edge_item<T, M, D>(a, item);
 }
 
-// Same pass over a work list, by a fixed grid of warps.
+// Same pass over a work list (sorted by item, so lower positions go first), by a
+// fixed grid of warps that take the next item from a shared ticket.
 template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_tie_edge_list(QueryArgs<T> a) {
-    const int nw = gridDim.x * 4;
     const int cnt = *a.n_wlist;
-    for (int wi = blockIdx.x * 4 + (threadIdx.x >> 5); wi < cnt; wi += nw) tie_edge_item<T, M, D>(a, a.wlist[wi]);
+    for (;;) {
+        int wi = 0;
+        if (lane_id() == 0) wi = atomicAdd(a.ticket, 1);
+        wi = __shfl_sync(0xffffffffu, wi, 0);
+        if (wi >= cnt) return;
+        tie_edge_item<T, M, D>(a, a.wlist[wi]);
+    }
 }
 
 // Pointer jumping: L(p) - 1 is reachable from p, so L(p) may take L(L(p) - 1).
@@ -600,7 +635,8 @@ __global__ void k_tie_cell_min(QueryArgs<T> a) {
 }
 
 // Next pass's work: the items of every cell whose lower stencil or own cell was
-// dirtied in this pass (each cell once per pass), warp per dirty cell.
+// dirtied in this pass are flagged (warp per dirty cell); k_tie_compact then lists the
+// flagged items in increasing order.
 template <typename T>
 __global__ void __launch_bounds__(128) k_tie_schedule(QueryArgs<T> a) {
     const int nw = gridDim.x * 4;
@@ -612,29 +648,36 @@ __global__ void __launch_bounds__(128) k_tie_schedule(QueryArgs<T> a) {
             const int rep_c = a.cell_rep[cr];
             if (rep_c == kNoCore) return true;
             if ((a.cell_flags[cr] & kCellUniform) && a.tmax[a.parent[rep_c]] < a.ct.start[cr]) return true;
-            int base = -1, nit = 0, first = 0;
-            if (lane == 0 && atomicMax(a.sched_gen + cr, a.gen) < a.gen) {
-                const int s0 = a.ct.start[cr];
-                nit = (a.ct.start[cr + 1] - s0 + 31) >> 5;
-                first = (int)a.ipos[s0];
-                base = atomicAdd(a.n_wlist_out, nit);
-            }
-            base = __shfl_sync(0xffffffffu, base, 0);
-            nit = __shfl_sync(0xffffffffu, nit, 0);
-            first = __shfl_sync(0xffffffffu, first, 0);
-            for (int k = (int)lane; base >= 0 && k < nit; k += 32) a.wlist_out[base + k] = first + k;
+            int fresh = 0;
+            if (lane == 0) fresh = atomicMax(a.sched_gen + cr, a.gen) < a.gen;
+            if (!__shfl_sync(0xffffffffu, fresh, 0)) return true;
+            const int s0 = a.ct.start[cr];
+            const int nit = (a.ct.start[cr + 1] - s0 + 31) >> 5;
+            const int first = (int)a.ipos[s0];
+            for (int k = (int)lane; k < nit; k += 32) a.item_flag[first + k] = 1u;
             return true;
+        }, false, [&](int cr) {
+            const int rep_c = a.cell_rep[cr];
+            if (rep_c == kNoCore) return false;
+            return !((a.cell_flags[cr] & kCellUniform) && a.tmax[a.parent[rep_c]] < a.ct.start[cr]);
         });
+    }
+}
+
+// Lists the flagged items in increasing order (pos = exclusive scan of the flags)
+// and clears the flags for the next pass.
+static __global__ void k_tie_compact(uint32_t* item_flag, const uint32_t* pos, int n_items, int* wlist) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_items && item_flag[i]) {
+        wlist[pos[i]] = i;
+        item_flag[i] = 0u;
     }
 }
 
 // Greedy descent step: g(p) = some core eps-neighbour below p (p itself if none).
 // Any decreasing core edge leads to a position reachable from p, so following g
 // from p (pointer jumping) ends at an upper bound of L(p) - 1, equal to the
-// component root whenever the descent reaches it.  To descend fast the lower cell
-// across the most significant dimension (all of whose points lie below the whole
-// slice of p) is tried first, then the other lower cells, then the own cell; each
-// lane stops at its first hit.
+// component root whenever the descent reaches it.  Each lane stops at its first hit.
 template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_tie_greedy(QueryArgs<T> a) {
     const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
@@ -657,23 +700,20 @@ __global__ void __launch_bounds__(128) k_tie_greedy(QueryArgs<T> a) {
         if (within<T, M, D>(a, q, tile, u)) { g = qi; found = true; }
     };
     auto done = [&]() { return __all_sync(0xffffffffu, found); };
-    // the lower face across the most significant dimension
+    // lower positions of the own cell first (most pairs inside a cell are within eps),
+    // then the lower face across the most significant dimension, then the rest
+    bool all = scan_range(a, tile, a.ct.start[r], pend, aux_of, pair, done);
     const int top = a.g.d - 1;
     const unsigned long long key = a.ct.key[r];
     int face = -1;
-    if (a.ct.ccoord[(size_t)top * a.ct.pitch + r] > 0) face = find_cell(a.ct, key - a.g.stride[top]);
-    bool all = false;
+    if (!all && a.ct.ccoord[(size_t)top * a.ct.pitch + r] > 0) face = find_cell(a.ct, key - a.g.stride[top]);
     if (face >= 0 && a.cell_rep[face] != kNoCore)
         all = scan_range(a, tile, a.ct.start[face], a.ct.start[face + 1], aux_of, pair, done);
     if (!all) {
         visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
-            if (own) {
-                scan_range(a, tile, a.ct.start[r], pend, aux_of, pair, done);
-                return true;
-            }
-            if (cr == face || a.cell_rep[cr] == kNoCore) return true;
+            if (own || cr == face || a.cell_rep[cr] == kNoCore) return true;
             return !scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
-        }, /*own_last=*/true);
+        });
     }
     if (active) a.lm1[p] = g;
 }
