@@ -412,6 +412,14 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
             HPD_CU(cudaStreamSynchronize(s));
             info.launches += 1;
             if (trace) fprintf(stderr, "[hpd tie] pass %d work %d undecided %d\n", pass, h_work, h_left);
+            if (h_left > 0 && !converged) {
+                // only the components next to the borders still undecided need values
+                a.amb = lists[cur];
+                a.n_amb = counts[cur];
+                HPD_CU(cudaMemsetAsync(tmax, 0xff, (size_t)n * sizeof(int), s));
+                HPD_QUERY_DISPATCH(k_tie_mark, T, mode, d, blocks_for(h_left, 4), 128, 0, s, a);
+                info.launches += 1;
+            }
         }
         info.tie_iterations = pass;
     }
