@@ -32,12 +32,15 @@ struct Arena {
     bool fixed = false;  // wraps memory it does not own: never allocates or frees
     cudaError_t reserve(size_t bytes);
     void reset() { used = 0; }
+    // Hands out the next 256-byte aligned block; the caller reserves enough for all
+    // its blocks (size + 256 each) and checks overflowed() once after the last take.
     template <typename T>
     T* take(size_t count) {
         size_t off = (used + 255) & ~size_t(255);
         used = off + count * sizeof(T);
         return reinterpret_cast<T*>(static_cast<char*>(ptr) + off);
     }
+    bool overflowed() const { return used > cap; }
     ~Arena();
 };
 

@@ -48,6 +48,8 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
         }                                                                                                    \
     } while (0)
 
+constexpr int kDenseMinPoints = 128;
+
 template <typename T, typename K>
 int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, std::string& err, const Grid& g,
                    const T* mins, bool dense_ok);
@@ -72,6 +74,10 @@ int run_pipeline(const Request& rq, Arena& small, Arena& main, Timers* tm, RunIn
     T* pmax = small.take<T>((size_t)nblk * d);
     T* ext = small.take<T>(2 * d);
     int* bad = small.take<int>(1);
+    if (small.overflowed()) {
+        err = "internal error: device buffer plan exceeds its reservation";
+        return kRuntime;
+    }
     HPD_CU(cudaMemsetAsync(bad, 0, sizeof(int), s));
     k_minmax_partial<T><<<nblk, tpb, 2 * tpb * sizeof(T), s>>>(static_cast<const T*>(rq.d_data), count, d, pmin, pmax, bad);
     k_minmax_final<T><<<1, 32, 0, s>>>(pmin, pmax, nblk, d, ext);
@@ -154,9 +160,26 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     need += (size_t)n + 5 * (size_t)n * 4;                           // core, tmax, parent, broot, lm1, amb
     need += (size_t)n * 4 + (size_t)n;                               // cell rep, cell flags
     need += 9 * (size_t)n * 4;                                       // dirty / schedule stamps, dirty list, work lists, cell / item min, item flags
+    // dense cells: sub-cells per dimension (0: path off), see k_dense_group
+    int dense_k = 0;
+    if (Elem<T>::kFloat && d <= 4) {
+        double err = 0;
+        for (int k = 0; k < d; ++k)
+            err = std::max(err, (std::fabs((double)mins[k]) + (double)g.dims[k] * (double)rq.eps) * std::ldexp(1.0, -20));
+        for (int kk = 2; kk <= 3 && !dense_k; ++kk) {
+            int groups = 1;
+            for (int k = 0; k < d; ++k) groups *= kk;
+            if (groups <= 81 && std::sqrt((double)d) * ((double)rq.eps / kk + 4 * err) <= 0.95 * (double)rq.eps)
+                dense_k = kk;
+        }
+    }
+    int dense_groups = 1;
+    for (int k = 0; k < d; ++k) dense_groups *= std::max(dense_k, 1);
+    const int64_t dense_max = (int64_t)n / kDenseMinPoints + 1;
+    need += 3 * (size_t)n * 4 + (size_t)dense_max * (2 * dense_groups + 2) * 4;  // dense-cell tables
     need += (size_t)n * 4;                                           // second ambiguous list
     need += (size_t)ncounts * 4 + (size_t)nscan * 8 + 64;
-    need += 32 * 256;                                                // alignment slack
+    need += 64 * 256;                                                // alignment of up to 64 blocks
     HPD_CU(main.reserve(need));
     main.reset();
     K* keys = main.take<K>(n);
@@ -190,11 +213,21 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     int* cell_min_l = main.take<int>(n);
     int* item_min_l = main.take<int>(n);
     uint32_t* item_flag = main.take<uint32_t>(n);
+    int* dense_id = main.take<int>(n);
+    int* dense_cells = main.take<int>(dense_max);
+    int* dense_grp = main.take<int>((size_t)dense_max * (dense_groups + 1));
+    int* dense_rep = main.take<int>((size_t)dense_max * dense_groups);
+    int* dense_sec = main.take<int>(n);
+    int* dense_gidx = main.take<int>(n);
     uint32_t* item_pos = main.take<uint32_t>(n);
     uint32_t* counts = main.take<uint32_t>(ncounts);
     uint32_t* scan32 = main.take<uint32_t>(2 * nscan);
     uint32_t* totals = main.take<uint32_t>(4);   // cells, items
     int* flags_dev = main.take<int>(16);          // list counters, diagnostics
+    if (main.overflowed()) {
+        err = "internal error: device buffer plan exceeds its reservation";
+        return kRuntime;
+    }
 
     // ---- cell ids (spatial_index.h:144-165)
     CellParams cp;
@@ -277,6 +310,29 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
 
     // ---- core-core connectivity
     k_iota<<<blocks_for(n, 256), 256, 0, s>>>(parent, n);
+    if (dense_k > 0) {
+        DenseArgs da;
+        memset(&da, 0, sizeof da);
+        da.k = dense_k;
+        da.groups = 1;
+        for (int k = 0; k < d; ++k) da.groups *= dense_k;
+        da.min_points = kDenseMinPoints;
+        da.scale = (double)dense_k / (double)rq.eps;
+        for (int k = 0; k < d; ++k) da.mins_d[k] = (double)mins[k];
+        da.dense_id = dense_id;
+        da.cells = dense_cells;
+        da.n_dense = flags_dev + 12;
+        da.grp = dense_grp;
+        da.grp_rep = dense_rep;
+        da.sec = dense_sec;
+        da.gidx = dense_gidx;
+        HPD_CU(cudaMemsetAsync(da.n_dense, 0, sizeof(int), s));
+        k_dense_list<<<blocks_for(m, 256), 256, 0, s>>>(cell_start, m, da);
+        k_dense_group<T><<<(unsigned)dense_max, 256, 0, s>>>(a, da);
+        HPD_QUERY_DISPATCH(k_dense_pairs, T, mode, d, blocks_for(dense_max, 4), 128, 0, s, a, da);
+        a.dense_id = dense_id;
+        info.launches += 3;
+    }
     HPD_QUERY_DISPATCH(k_union_intra, T, mode, d, qgrid, 128, qsmem, s, a);
     k_fill_int<<<blocks_for(m, 256), 256, 0, s>>>(cell_rep, m, kNoCore);
     HPD_CU(cudaMemsetAsync(cell_flags, kCellUniform, m, s));

@@ -143,6 +143,7 @@ struct QueryArgs {
     uint32_t* item_flag;  // items scheduled for the next pass
     int* ticket;          // next work-list entry to take
     unsigned long long* trace_counts;  // diagnostics (nullptr: off): [0] active lanes, [1] tiles scanned
+    const int* dense_id;  // per cell: >= 0 when the dense-cell kernels connect its cores
     int* amb_out;         // undecided ambiguous borders after a decision round
     int* n_amb_out;
 };
@@ -288,6 +289,7 @@ __global__ void __launch_bounds__(128) k_union_intra(QueryArgs<T> a) {
     if (item >= a.n_items) return;
     const int2 it = a.items[item];
     const int r = it.x;
+    if (a.dense_id && a.dense_id[r] >= 0) return;  // connected by the dense-cell kernels
     const int pend = min(it.y + 32, a.ct.start[r + 1]);
     const int p = it.y + (int)lane_id();
     const bool active = p < pend && a.core[p];
@@ -319,6 +321,144 @@ static __global__ void k_cell_uniform(const uint8_t* core, int* parent, const ui
     if (i < n && core[i]) {
         const uint32_t c = cellrank[i];
         if (uf_find(parent, i) != cell_rep[c]) cell_flags[c] = 0;
+    }
+}
+
+// ------------------------------------------------------ dense cells
+// A cell holding many points is split into k^d sub-cells of side eps / k, with k
+// chosen on the host so that the diagonal of a sub-cell, widened by the rounding
+// slack of the cell computation, is at most 0.95 eps: any two points of one sub-cell
+// are then within eps under the reference's arithmetic (the computed squared
+// distance stays ~10 % below EPS2), so the cores of a sub-cell form a clique and are
+// united as a star.  Sub-cells of one cell are then connected pairwise by a
+// first-hit scan unless already in one component.  Connectivity is exactly that of
+// the core-core eps graph inside the cell, at O(points) cost instead of O(points^2).
+struct DenseArgs {
+    int k;                  // sub-cells per dimension
+    int groups;             // k^d
+    int min_points;         // cells with at least this many points take this path
+    double scale;           // k / eps
+    double mins_d[kMaxDims];
+    int* dense_id;          // per cell: index in the dense list or -1
+    int* cells;             // dense list: cell rank
+    int* n_dense;
+    int* grp;               // [dense][groups + 1] start of each sub-cell in sec (relative to the cell)
+    int* grp_rep;           // [dense][groups] smallest core of each sub-cell (INT_MAX: none)
+    int* sec;               // points of dense cells grouped by sub-cell (same range as the cell)
+    int* gidx;              // per point of a dense cell: its sub-cell
+};
+
+static __global__ void k_dense_list(const int32_t* cell_start, int m, DenseArgs da) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m) return;
+    if (cell_start[c + 1] - cell_start[c] >= da.min_points) {
+        const int id = atomicAdd(da.n_dense, 1);
+        da.dense_id[c] = id;
+        da.cells[id] = c;
+    } else {
+        da.dense_id[c] = -1;
+    }
+}
+
+// block per dense cell: sub-cell of every point, counting sort into sec, star roots
+template <typename T>
+__global__ void __launch_bounds__(256) k_dense_group(QueryArgs<T> a, DenseArgs da) {
+    __shared__ int cnt[256];
+    __shared__ int cur[256];
+    const int id = blockIdx.x;
+    if (id >= *da.n_dense) return;
+    const int c = da.cells[id];
+    const int s0 = a.ct.start[c], s1 = a.ct.start[c + 1];
+    for (int g = threadIdx.x; g < da.groups; g += blockDim.x) {
+        cnt[g] = 0;
+        da.grp_rep[(size_t)id * da.groups + g] = INT_MAX;
+    }
+    __syncthreads();
+    for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+        int g = 0, mul = 1;
+        for (int sd = 0; sd < a.g.d; ++sd) {
+            const int j = a.g.swapped[sd];
+            const double v = ((double)a.coords[(size_t)j * a.n + i] - da.mins_d[j]) * da.scale;
+            long long sub = (long long)floor(v) - (long long)da.k * (long long)a.ct.ccoord[(size_t)sd * a.ct.pitch + c];
+            sub = sub < 0 ? 0 : (sub >= da.k ? da.k - 1 : sub);
+            g += (int)sub * mul;
+            mul *= da.k;
+        }
+        da.gidx[i] = g;
+        atomicAdd(&cnt[g], 1);
+        if (a.core[i]) atomicMin(&da.grp_rep[(size_t)id * da.groups + g], i);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int g = 0; g < da.groups; ++g) {
+            da.grp[(size_t)id * (da.groups + 1) + g] = run;
+            cur[g] = run;
+            run += cnt[g];
+        }
+        da.grp[(size_t)id * (da.groups + 1) + da.groups] = run;
+    }
+    __syncthreads();
+    for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+        const int g = da.gidx[i];
+        da.sec[s0 + atomicAdd(&cur[g], 1)] = i;
+        // star union inside the sub-cell: the smallest core is a root at this point
+        if (a.core[i]) {
+            const int rep = da.grp_rep[(size_t)id * da.groups + g];
+            if (rep != i) a.parent[i] = rep;
+        }
+    }
+}
+
+template <typename T, int M, int D>
+__device__ __forceinline__ bool within_pts(const QueryArgs<T>& a, int i, int j) {
+    T t[D > 0 ? D : kMaxDims];
+#pragma unroll
+    for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+        if (D == 0 && k >= a.g.d) break;
+        t[k] = sub_(a.coords[(size_t)k * a.n + i], a.coords[(size_t)k * a.n + j]);
+    }
+    return fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
+}
+
+__device__ __forceinline__ bool same_component(int* parent, int x, int y);
+
+// warp per dense cell: connect its sub-cells pairwise (first core-core eps pair found)
+template <typename T, int M, int D>
+__global__ void __launch_bounds__(128) k_dense_pairs(QueryArgs<T> a, DenseArgs da) {
+    const int id = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (id >= *da.n_dense) return;
+    const unsigned lane = lane_id();
+    const int c = da.cells[id];
+    const int s0 = a.ct.start[c];
+    const int* grp = da.grp + (size_t)id * (da.groups + 1);
+    const int* rep = da.grp_rep + (size_t)id * da.groups;
+    for (int g1 = 0; g1 < da.groups; ++g1) {
+        if (rep[g1] == INT_MAX) continue;
+        for (int g2 = g1 + 1; g2 < da.groups; ++g2) {
+            if (rep[g2] == INT_MAX) continue;
+            if (same_component(a.parent, rep[g1], rep[g2])) continue;
+            bool joined = false;
+            for (int x = grp[g1]; x < grp[g1 + 1] && !joined; ++x) {
+                const int pa = da.sec[s0 + x];
+                if (!a.core[pa]) continue;
+                for (int y0 = grp[g2]; y0 < grp[g2 + 1] && !joined; y0 += 32) {
+                    const int y = y0 + (int)lane;
+                    int pb = -1;
+                    if (y < grp[g2 + 1]) {
+                        pb = da.sec[s0 + y];
+                        if (!a.core[pb] || !within_pts<T, M, D>(a, pa, pb)) pb = -1;
+                    }
+                    const unsigned hit = __ballot_sync(0xffffffffu, pb >= 0);
+                    if (hit) {
+                        const int other = __shfl_sync(0xffffffffu, pb, __ffs(hit) - 1);
+                        if (lane == 0) uf_union(a.parent, pa, other);
+                        __syncwarp();
+                        joined = true;
+                    }
+                }
+            }
+        }
     }
 }
 
