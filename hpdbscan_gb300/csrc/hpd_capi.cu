@@ -67,6 +67,14 @@ int run(hpd_handle* h, const void* d_data, int64_t n, int32_t d, int32_t dtype, 
     switch (dtype) {
         case HPD_F32: rc = run_pipeline<float>(rq, h->small, h->main, &h->timers, h->last, err); break;
         case HPD_F64: rc = run_pipeline<double>(rq, h->small, h->main, &h->timers, h->last, err); break;
+        case HPD_I8: rc = run_pipeline<int8_t>(rq, h->small, h->main, &h->timers, h->last, err); break;
+        case HPD_I16: rc = run_pipeline<int16_t>(rq, h->small, h->main, &h->timers, h->last, err); break;
+        case HPD_I32: rc = run_pipeline<int32_t>(rq, h->small, h->main, &h->timers, h->last, err); break;
+        case HPD_I64: rc = run_pipeline<int64_t>(rq, h->small, h->main, &h->timers, h->last, err); break;
+        case HPD_U8: rc = run_pipeline<uint8_t>(rq, h->small, h->main, &h->timers, h->last, err); break;
+        case HPD_U16: rc = run_pipeline<uint16_t>(rq, h->small, h->main, &h->timers, h->last, err); break;
+        case HPD_U32: rc = run_pipeline<uint32_t>(rq, h->small, h->main, &h->timers, h->last, err); break;
+        case HPD_U64: rc = run_pipeline<uint64_t>(rq, h->small, h->main, &h->timers, h->last, err); break;
         default: return fail(HPD_ERR_UNSUPPORTED, "element type not supported by this build");
     }
     if (rc != HPD_OK) return fail(rc, err);

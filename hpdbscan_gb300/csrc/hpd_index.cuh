@@ -5,6 +5,8 @@
 
 #include <cfloat>
 #include <climits>
+#include <cstdint>
+#include <type_traits>
 
 #include "hpd_common.cuh"
 
@@ -20,22 +22,66 @@ template <> struct Elem<float> {
     static constexpr bool kFloat = true;
     __host__ __device__ static float lowest_for_max() { return FLT_MIN; }  // numeric_limits<float>::min()
     __host__ __device__ static float highest() { return FLT_MAX; }
+    __host__ __device__ static float lowest() { return -FLT_MAX; }
 };
 template <> struct Elem<double> {
     using F = double;
     static constexpr bool kFloat = true;
     __host__ __device__ static double lowest_for_max() { return DBL_MIN; }
     __host__ __device__ static double highest() { return DBL_MAX; }
+    __host__ __device__ static double lowest() { return -DBL_MAX; }
 };
+// Integer element types: numeric_limits<T>::min() is the most negative value (0 for
+// unsigned), so the reference's max initialiser is simply the type's minimum.
+#define HPD_INT_ELEM(T, LO, HI)                                                  \
+    template <> struct Elem<T> {                                                 \
+        using F = float;                                                         \
+        static constexpr bool kFloat = false;                                    \
+        __host__ __device__ static T lowest_for_max() { return LO; }            \
+        __host__ __device__ static T highest() { return HI; }                   \
+        __host__ __device__ static T lowest() { return LO; }                    \
+    };
+HPD_INT_ELEM(int8_t, INT8_MIN, INT8_MAX)
+HPD_INT_ELEM(int16_t, INT16_MIN, INT16_MAX)
+HPD_INT_ELEM(int32_t, INT32_MIN, INT32_MAX)
+HPD_INT_ELEM(int64_t, INT64_MIN, INT64_MAX)
+HPD_INT_ELEM(uint8_t, 0, UINT8_MAX)
+HPD_INT_ELEM(uint16_t, 0, UINT16_MAX)
+HPD_INT_ELEM(uint32_t, 0, UINT32_MAX)
+HPD_INT_ELEM(uint64_t, 0, UINT64_MAX)
+#undef HPD_INT_ELEM
 
-// (x - mn) as the reference evaluates it, in the float type F.
+// (x - mn) as the reference evaluates it, in the float type F: for integer T the
+// difference is taken in the promoted type (int below 32 bits, else T itself, which
+// wraps) and converted to float with round-to-nearest.
 template <typename T>
 __host__ __device__ __forceinline__ typename Elem<T>::F diff_f(T x, T mn) {
 #ifdef __CUDA_ARCH__
-    return sub_(x, mn);
+    if constexpr (Elem<T>::kFloat) return sub_(x, mn);
 #else
-    return x - mn;  // host code is compiled without contraction or fast-math
+    if constexpr (Elem<T>::kFloat) return x - mn;  // host code is compiled without contraction or fast-math
 #endif
+    else if constexpr (sizeof(T) < 4) return (float)((int)x - (int)mn);
+    else if constexpr (std::is_signed<T>::value && sizeof(T) == 4) return (float)(int32_t)((uint32_t)x - (uint32_t)mn);
+    else if constexpr (std::is_signed<T>::value) return (float)(int64_t)((uint64_t)x - (uint64_t)mn);
+    else return (float)(T)(x - mn);
+}
+
+// EPS2 = (T)(float)(eps * eps) (hpdbscan.h:53 then the region query's T parameter),
+// with the conversions GCC emits for the narrow integer types.
+template <typename T>
+__host__ __device__ __forceinline__ T eps2_of(float eps) {
+    const float e2 = eps * eps;
+    if constexpr (Elem<T>::kFloat) return (T)e2;
+    else if constexpr (sizeof(T) < 4) return (T)(int32_t)e2;
+    else if constexpr (std::is_same<T, uint32_t>::value) return (T)(int64_t)e2;
+    else return (T)e2;
+}
+
+template <typename T>
+__device__ __forceinline__ bool nonfinite(T c) {
+    if constexpr (Elem<T>::kFloat) return !isfinite(c);
+    else return false;
 }
 
 // floor((x - mn) / eps) with the reference's rounding, as an unsigned cell index.
@@ -66,15 +112,15 @@ __global__ void k_minmax_partial(const T* __restrict__ data, int64_t count, int 
     T* smin = reinterpret_cast<T*>(smem_raw);
     T* smax = smin + blockDim.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    T mn = Elem<T>::highest(), mx = -Elem<T>::highest();
-    bool nonfinite = false;
+    T mn = Elem<T>::highest(), mx = Elem<T>::lowest();
+    bool bad_value = false;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += stride) {
         T c = data[e];
-        if (Elem<T>::kFloat && !isfinite(c)) nonfinite = true;
+        if (nonfinite(c)) bad_value = true;
         if (c < mn) mn = c;
         if (mx < c) mx = c;
     }
-    if (nonfinite) atomicExch(bad, 1);
+    if (bad_value) atomicExch(bad, 1);
     smin[threadIdx.x] = mn;
     smax[threadIdx.x] = mx;
     __syncthreads();
@@ -93,7 +139,7 @@ __global__ void k_minmax_final(const T* __restrict__ pmin, const T* __restrict__
                                T* __restrict__ out /* [2d]: mins, maxs */) {
     const int k = threadIdx.x;
     if (k >= d) return;
-    T mn = Elem<T>::highest(), mx = -Elem<T>::highest();
+    T mn = Elem<T>::highest(), mx = Elem<T>::lowest();
     for (int b = 0; b < nblocks; ++b) {
         T a = pmin[(int64_t)b * d + k], c = pmax[(int64_t)b * d + k];
         if (a < mn) mn = a;
@@ -106,7 +152,7 @@ __global__ void k_minmax_final(const T* __restrict__ pmin, const T* __restrict__
 // ------------------------------------------------------------- cell ids
 struct CellParams {
     Grid g;
-    double mins_d[kMaxDims];  // per original dimension, stored as double (exact for float/double)
+    unsigned long long mins_raw[kMaxDims];  // per original dimension: the bytes of the T minimum
     double eps;
     double recip;
     int cell_mode;
@@ -123,7 +169,9 @@ __global__ void k_cell_keys(const T* __restrict__ data, int64_t n, CellParams cp
     unsigned long long key = 0;
     for (int s = 0; s < d; ++s) {
         const int k = cp.g.swapped[s];
-        key += cell_coord<T>(p[k], (T)cp.mins_d[k], (F)cp.eps, (F)cp.recip, cp.cell_mode) * cp.g.stride[s];
+        T mn;
+        memcpy(&mn, &cp.mins_raw[k], sizeof(T));
+        key += cell_coord<T>(p[k], mn, (F)cp.eps, (F)cp.recip, cp.cell_mode) * cp.g.stride[s];
     }
     keys[i] = (K)key;
     idx[i] = (int32_t)i;

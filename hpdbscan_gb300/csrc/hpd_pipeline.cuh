@@ -35,20 +35,25 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
 // GCC x86-64 order equals the sequential order.
 #define HPD_QUERY_DISPATCH(KERNEL, T, mode, d, grid, block, smem, stream, ...)                                 \
     do {                                                                                                     \
-        if ((d) == 2) {                                                                                      \
-            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 2><<<grid, block, smem, stream>>>(__VA_ARGS__);       \
-            else KERNEL<T, kDistSeq, 2><<<grid, block, smem, stream>>>(__VA_ARGS__);                                \
+        if constexpr (!Elem<T>::kFloat) {                                                                    \
+            /* integer sums wrap, so every summation order gives the same result */                          \
+            if ((d) == 2) KERNEL<T, kDistSeq, 2><<<grid, block, smem, stream>>>(__VA_ARGS__);                \
+            else if ((d) == 3) KERNEL<T, kDistSeq, 3><<<grid, block, smem, stream>>>(__VA_ARGS__);           \
+            else KERNEL<T, kDistSeq, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
+        } else if ((d) == 2) {                                                                               \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 2><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else KERNEL<T, kDistSeq, 2><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
         } else if ((d) == 3) {                                                                               \
-            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 3><<<grid, block, smem, stream>>>(__VA_ARGS__);       \
-            else KERNEL<T, kDistSeq, 3><<<grid, block, smem, stream>>>(__VA_ARGS__);                                \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 3><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else KERNEL<T, kDistSeq, 3><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
         } else {                                                                                             \
-            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);       \
-            else if ((mode) == kDistSeq) KERNEL<T, kDistSeq, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);        \
-            else KERNEL<T, kDistGccX86, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);                             \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 0><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else if ((mode) == kDistSeq) KERNEL<T, kDistSeq, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);  \
+            else KERNEL<T, kDistGccX86, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);                      \
         }                                                                                                    \
     } while (0)
 
-constexpr int kDenseMinPoints = 128;
+constexpr int kDenseMinPoints = 128;  // cells with this many points take the dense-cell path
 
 template <typename T, typename K>
 int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, std::string& err, const Grid& g,
@@ -233,7 +238,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     CellParams cp;
     memset(&cp, 0, sizeof cp);
     cp.g = g;
-    for (int k = 0; k < d; ++k) cp.mins_d[k] = (double)mins[k];
+    for (int k = 0; k < d; ++k) memcpy(&cp.mins_raw[k], &mins[k], sizeof(T));
     cp.eps = (double)(F)rq.eps;
     cp.recip = (double)((F)1 / (F)rq.eps);
     cp.cell_mode = rq.cell_mode;
@@ -278,7 +283,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     a.ct.m = m;
     a.ct.ccoord = ccoord;
     a.ct.pitch = n;
-    a.eps2 = (T)(rq.eps * rq.eps);  // const float EPS2 = eps * eps (hpdbscan.h:53), converted to T
+    a.eps2 = eps2_of<T>(rq.eps);  // const float EPS2 = eps * eps (hpdbscan.h:53), converted to T
     a.items = items;
     a.n_items = n_items;
     a.min_points = (int)std::min<uint64_t>(rq.min_points, (uint64_t)n + 1);

@@ -13,6 +13,7 @@
 #include <climits>
 
 #include "hpd_common.cuh"
+#include "hpd_index.cuh"
 
 namespace hpd {
 
@@ -198,7 +199,14 @@ __device__ __forceinline__ bool scan_range(const QueryArgs<T>& a, const Tile<T>&
 // candidate u of the tile into c[] (vector loads for d = 2..4)
 template <typename T, int D>
 __device__ __forceinline__ void tile_load(const Tile<T>& tile, int u, int d, T* c) {
-    if (D == 2) {
+    if constexpr (!Elem<T>::kFloat) {
+        const int S = tile_stride(d);
+#pragma unroll
+        for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+            if (D == 0 && k >= d) break;
+            c[k] = tile.c[u * S + k];
+        }
+    } else if (D == 2) {
         if (sizeof(T) == 4) { const float2 v = reinterpret_cast<const float2*>(tile.c)[u]; c[0] = (T)v.x; c[1] = (T)v.y; }
         else { const double2 v = reinterpret_cast<const double2*>(tile.c)[u]; c[0] = (T)v.x; c[1] = (T)v.y; }
     } else if (D == 3 || D == 4) {
@@ -222,18 +230,38 @@ __device__ __forceinline__ void tile_load(const Tile<T>& tile, int u, int d, T* 
     }
 }
 
+// Integer element types: `T distance = p - q; offset += distance * distance`
+// (spatial_index.h:751-754) wraps at every store into T, so the result is the sum of
+// the wrapped squares modulo 2^bits(T), read back as T, in any summation order.
+template <typename T, int D>
+__device__ __forceinline__ bool int_within(const T* p, const T* q, int d, T eps2) {
+    unsigned long long acc = 0;
+#pragma unroll
+    for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+        if (D == 0 && k >= d) break;
+        const T t = (T)((unsigned long long)p[k] - (unsigned long long)q[k]);
+        const unsigned long long w = (unsigned long long)(long long)t;
+        acc += w * w;
+    }
+    return (T)acc <= eps2;
+}
+
 // squared distance from the lane's query (q[]) to tile slot u, compared with eps2
 template <typename T, int M, int D>
 __device__ __forceinline__ bool within(const QueryArgs<T>& a, const T* q, const Tile<T>& tile, int u) {
     T c[D > 0 ? (D < 4 ? 4 : D) : kMaxDims];
     tile_load<T, D>(tile, u, a.g.d, c);
-    T t[D > 0 ? D : kMaxDims];
+    if constexpr (!Elem<T>::kFloat) {
+        return int_within<T, D>(q, c, a.g.d, a.eps2);
+    } else {
+        T t[D > 0 ? D : kMaxDims];
 #pragma unroll
-    for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-        if (D == 0 && k >= a.g.d) break;
-        t[k] = sub_(q[k], c[k]);
+        for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+            if (D == 0 && k >= a.g.d) break;
+            t[k] = sub_(q[k], c[k]);
+        }
+        return fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
     }
-    return fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
 }
 
 template <typename T, int D>
@@ -412,13 +440,19 @@ __global__ void __launch_bounds__(256) k_dense_group(QueryArgs<T> a, DenseArgs d
 
 template <typename T, int M, int D>
 __device__ __forceinline__ bool within_pts(const QueryArgs<T>& a, int i, int j) {
-    T t[D > 0 ? D : kMaxDims];
+    if constexpr (!Elem<T>::kFloat) {
+        T x[D > 0 ? D : kMaxDims], y[D > 0 ? D : kMaxDims];
+        for (int k = 0; k < a.g.d; ++k) { x[k] = a.coords[(size_t)k * a.n + i]; y[k] = a.coords[(size_t)k * a.n + j]; }
+        return int_within<T, D>(x, y, a.g.d, a.eps2);
+    } else {
+        T t[D > 0 ? D : kMaxDims];
 #pragma unroll
-    for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-        if (D == 0 && k >= a.g.d) break;
-        t[k] = sub_(a.coords[(size_t)k * a.n + i], a.coords[(size_t)k * a.n + j]);
+        for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+            if (D == 0 && k >= a.g.d) break;
+            t[k] = sub_(a.coords[(size_t)k * a.n + i], a.coords[(size_t)k * a.n + j]);
+        }
+        return fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
     }
-    return fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
 }
 
 __device__ __forceinline__ bool same_component(int* parent, int x, int y);
@@ -585,13 +619,25 @@ __device__ __forceinline__ void scan_point(const QueryArgs<T>& a, int p, Hit&& h
         const int ce = a.ct.start[cr + 1];
         for (int j = a.ct.start[cr] + (int)lane; j < ce; j += 32) {
             if (!a.core[j]) continue;
-            T t[D > 0 ? D : kMaxDims];
+            T c[D > 0 ? D : kMaxDims];
 #pragma unroll
             for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
                 if (D == 0 && k >= a.g.d) break;
-                t[k] = sub_(q[k], a.coords[(size_t)k * a.n + j]);
+                c[k] = a.coords[(size_t)k * a.n + j];
             }
-            if (fold_sq<T, M, D>(t, a.g.d) <= a.eps2) hit(j);
+            bool in;
+            if constexpr (!Elem<T>::kFloat) {
+                in = int_within<T, D>(q, c, a.g.d, a.eps2);
+            } else {
+                T t[D > 0 ? D : kMaxDims];
+#pragma unroll
+                for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                    if (D == 0 && k >= a.g.d) break;
+                    t[k] = sub_(q[k], c[k]);
+                }
+                in = fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
+            }
+            if (in) hit(j);
         }
         return true;
     });

@@ -22,6 +22,9 @@ Sets:
                      x / eps round to different cells
   edge_*             edge cases: all-negative dimension (the max-init quirk),
                      duplicates, one point, minPts 0 / 1 / > n, one big cell
+  int_<type>_d{2,3}  the eight integer element types (upstream instantiations), with
+                     coordinates and eps chosen so that the squared distances wrap
+                     around and EPS2 overflows the narrow types
 """
 from __future__ import annotations
 
@@ -140,6 +143,15 @@ def main():
     save("edge_minpts1", small, 0.05, 1)
     save("edge_minpts_big", small, 0.05, 5000)
     save("edge_one_cell", small, 10.0, 50)
+    rng = np.random.default_rng(11)
+    for dt, lo, hi, eps in [(np.int8, -128, 127, 30.0), (np.uint8, 0, 255, 9.5), (np.int16, -3000, 3000, 90.0),
+                            (np.uint16, 0, 60000, 1500.0), (np.int32, -100000, 100000, 4000.0),
+                            (np.uint32, 0, 4000000, 90000.0), (np.int64, -10**6, 10**6, 30000.0),
+                            (np.uint64, 0, 10**7, 2e5)]:
+        for d in (2, 3):
+            c = rng.integers(lo, hi, (8, d))
+            pts = np.clip(c[rng.integers(0, 8, 3000)] + rng.normal(0, eps, (3000, d)), lo, hi).astype(dt)
+            save(f"int_{np.dtype(dt).name}_d{d}", pts, eps, 6)
     manifest = {
         "reference_build": "upstream include/*.h via oracle/Makefile: g++ -std=c++11 -Ofast -fopenmp",
         "compiler": subprocess.run(["g++", "--version"], capture_output=True, text=True).stdout.splitlines()[0],
