@@ -36,7 +36,8 @@ class Stats(ctypes.Structure):
                 ("union_ms", ctypes.c_double), ("border_ms", ctypes.c_double), ("tie_ms", ctypes.c_double),
                 ("finalize_ms", ctypes.c_double),
                 ("n_cells", ctypes.c_int64), ("n_core", ctypes.c_int64), ("n_ambiguous", ctypes.c_int64),
-                ("tie_iterations", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+                ("tie_iterations", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
+                ("extent_ms", ctypes.c_double), ("cells_sort_ms", ctypes.c_double), ("cell_table_ms", ctypes.c_double)]
 
 
 _lib = None

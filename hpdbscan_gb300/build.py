@@ -20,6 +20,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhpdbscan_gb300.so")
+CLI = os.path.join(HERE, "hpdbscan")  # command line tool (csrc/hpdbscan_cli.cpp)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -73,6 +74,15 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
         os.replace(tmp, LIB)
+    cli_src = os.path.join(CSRC, "hpdbscan_cli.cpp")
+    if not os.path.exists(CLI) or os.path.getmtime(cli_src) > os.path.getmtime(CLI) or \
+            os.path.getmtime(LIB) > os.path.getmtime(CLI):
+        cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"), cli_src, "-o", CLI,
+               "-L", HERE, "-lhpdbscan_gb300", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError("CLI build failed")
     return LIB
 
 

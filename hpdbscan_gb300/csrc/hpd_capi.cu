@@ -179,6 +179,9 @@ int hpd_get_stats(const hpd_handle* h, hpd_stats* out) {
     out->border_ms = h->last.ms[4];
     out->tie_ms = h->last.ms[5];
     out->finalize_ms = h->last.ms[6];
+    out->extent_ms = h->last.index_ms[0];
+    out->cells_sort_ms = h->last.index_ms[1];
+    out->cell_table_ms = h->last.index_ms[2];
     out->n_cells = h->last.n_cells;
     out->n_core = h->last.n_core;
     out->n_ambiguous = h->last.n_ambiguous;

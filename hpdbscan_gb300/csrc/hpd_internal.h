@@ -45,7 +45,7 @@ struct Arena {
 };
 
 struct Timers {
-    cudaEvent_t ev[8] = {};
+    cudaEvent_t ev[10] = {};
     bool ok = false;
 };
 
@@ -66,6 +66,7 @@ struct RunInfo {
     int64_t n_cells = 0, n_core = 0, n_ambiguous = 0, tie_iterations = 0;
     int launches = 0;
     float ms[7] = {0, 0, 0, 0, 0, 0, 0};  // total, index, core, union, border, tie-break, finalize
+    float index_ms[3] = {0, 0, 0};          // extent, cell ids + sort, cell table
 };
 
 // Runs the whole pipeline for element type T.  Returns a Status and fills `err`.

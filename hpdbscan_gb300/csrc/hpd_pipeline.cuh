@@ -87,6 +87,7 @@ int run_pipeline(const Request& rq, Arena& small, Arena& main, Timers* tm, RunIn
     k_minmax_partial<T><<<nblk, tpb, 2 * tpb * sizeof(T), s>>>(static_cast<const T*>(rq.d_data), count, d, pmin, pmax, bad);
     k_minmax_final<T><<<1, 32, 0, s>>>(pmin, pmax, nblk, d, ext);
     info.launches += 2;
+    if (tm && tm->ok) HPD_CU(cudaEventRecord(tm->ev[7], s));
     T h_ext[2 * kMaxDims];
     int h_bad = 0;
     HPD_CU(cudaMemcpyAsync(h_ext, ext, 2 * d * sizeof(T), cudaMemcpyDeviceToHost, s));
@@ -254,6 +255,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         if (alt) { skeys = keys_alt; perm = vals_alt; }
     }
     k_gather<T><<<blocks_for(n, 256), 256, 0, s>>>(data, n, d, perm, coords);
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[8], s));
 
     // ---- cell table (spatial_index.h:167-182) and work items
     if (dense) HPD_CU(cudaMemsetAsync(dense, 0xff, (size_t)g.total * 4, s));
@@ -499,6 +501,9 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
             cudaEventElapsedTime(&ms, tm->ev[k - 1], tm->ev[k]);
             info.ms[k] = ms;
         }
+        cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[7]); info.index_ms[0] = ms;
+        cudaEventElapsedTime(&ms, tm->ev[7], tm->ev[8]); info.index_ms[1] = ms;
+        cudaEventElapsedTime(&ms, tm->ev[8], tm->ev[1]); info.index_ms[2] = ms;
     }
     return kOk;
 }

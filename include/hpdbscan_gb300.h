@@ -76,6 +76,9 @@ typedef struct {
     int64_t n_ambiguous; /* border points adjacent to >= 2 clusters */
     int64_t tie_iterations;
     int64_t kernel_launches;
+    double extent_ms;      /* part of index_ms: per-dimension min / max */
+    double cells_sort_ms;  /* part of index_ms: cell ids, radix sort, gather */
+    double cell_table_ms;  /* part of index_ms: cell table and work items */
 } hpd_stats;
 
 /* HPDBSCAN(epsilon, min_points): fails with HPD_ERR_INVALID and the upstream
