@@ -304,22 +304,10 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     const unsigned qgrid = blocks_for(n_items, 4);
     const size_t qsmem = 4 * ((size_t)tile_stride(d) * 32 * sizeof(T) + 32 * sizeof(int));
 
-    // ---- core test (hpdbscan.h:72-78)
-    if (rq.min_points <= 1) {
-        HPD_CU(cudaMemsetAsync(core, 1, n, s));
-    } else if (rq.min_points > (uint64_t)n) {
-        HPD_CU(cudaMemsetAsync(core, 0, n, s));
-    } else {
-        HPD_QUERY_DISPATCH(k_core, T, mode, d, qgrid, 128, qsmem, s, a);
-        info.launches += 1;
-    }
-    if (timed) HPD_CU(cudaEventRecord(tm->ev[2], s));
-
-    // ---- core-core connectivity
-    k_iota<<<blocks_for(n, 256), 256, 0, s>>>(parent, n);
+    // ---- dense cells: sub-cells (certified cliques) for the core test and the unions
+    DenseArgs da;
+    memset(&da, 0, sizeof da);
     if (dense_k > 0) {
-        DenseArgs da;
-        memset(&da, 0, sizeof da);
         da.k = dense_k;
         da.groups = 1;
         for (int k = 0; k < d; ++k) da.groups *= dense_k;
@@ -336,9 +324,30 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         HPD_CU(cudaMemsetAsync(da.n_dense, 0, sizeof(int), s));
         k_dense_list<<<blocks_for(m, 256), 256, 0, s>>>(cell_start, m, da);
         k_dense_group<T><<<(unsigned)dense_max, 256, 0, s>>>(a, da);
-        HPD_QUERY_DISPATCH(k_dense_pairs, T, mode, d, blocks_for(dense_max, 4), 128, 0, s, a, da);
         a.dense_id = dense_id;
-        info.launches += 3;
+        a.dense_grp = dense_grp;
+        a.dense_gidx = dense_gidx;
+        a.dense_groups = da.groups;
+        info.launches += 2;
+    }
+
+    // ---- core test (hpdbscan.h:72-78)
+    if (rq.min_points <= 1) {
+        HPD_CU(cudaMemsetAsync(core, 1, n, s));
+    } else if (rq.min_points > (uint64_t)n) {
+        HPD_CU(cudaMemsetAsync(core, 0, n, s));
+    } else {
+        HPD_QUERY_DISPATCH(k_core, T, mode, d, qgrid, 128, qsmem, s, a);
+        info.launches += 1;
+    }
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[2], s));
+
+    // ---- core-core connectivity
+    k_iota<<<blocks_for(n, 256), 256, 0, s>>>(parent, n);
+    if (dense_k > 0) {
+        k_dense_star<T><<<(unsigned)dense_max, 256, 0, s>>>(a, da);
+        HPD_QUERY_DISPATCH(k_dense_pairs, T, mode, d, blocks_for(dense_max, 4), 128, 0, s, a, da);
+        info.launches += 2;
     }
     HPD_QUERY_DISPATCH(k_union_intra, T, mode, d, qgrid, 128, qsmem, s, a);
     k_fill_int<<<blocks_for(m, 256), 256, 0, s>>>(cell_rep, m, kNoCore);

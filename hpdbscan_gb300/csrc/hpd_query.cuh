@@ -145,6 +145,9 @@ struct QueryArgs {
     int* ticket;          // next work-list entry to take
     unsigned long long* trace_counts;  // diagnostics (nullptr: off): [0] active lanes, [1] tiles scanned
     const int* dense_id;  // per cell: >= 0 when the dense-cell kernels connect its cores
+    const int* dense_grp; // [dense][groups + 1] sub-cell starts (see DenseArgs)
+    const int* dense_gidx;  // per point of a dense cell: its sub-cell
+    int dense_groups;
     int* amb_out;         // undecided ambiguous borders after a decision round
     int* n_amb_out;
 };
@@ -246,6 +249,22 @@ __device__ __forceinline__ bool int_within(const T* p, const T* q, int d, T eps2
     return (T)acc <= eps2;
 }
 
+// squared distance between q[] and c[] in the reference's arithmetic, <= eps2
+template <typename T, int M, int D>
+__device__ __forceinline__ bool within_vals(const QueryArgs<T>& a, const T* q, const T* c) {
+    if constexpr (!Elem<T>::kFloat) {
+        return int_within<T, D>(q, c, a.g.d, a.eps2);
+    } else {
+        T t[D > 0 ? D : kMaxDims];
+#pragma unroll
+        for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+            if (D == 0 && k >= a.g.d) break;
+            t[k] = sub_(q[k], c[k]);
+        }
+        return fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
+    }
+}
+
 // squared distance from the lane's query (q[]) to tile slot u, compared with eps2
 template <typename T, int M, int D>
 __device__ __forceinline__ bool within(const QueryArgs<T>& a, const T* q, const Tile<T>& tile, int u) {
@@ -276,9 +295,20 @@ __device__ __forceinline__ void load_query(const QueryArgs<T>& a, int p, bool ac
 // ---------------------------------------------------------------- core test
 // |N_eps(p)| >= minPoints, self included, with an early exit once every query of
 // the warp has reached minPoints (hpdbscan.h:74-78).
+template <typename T>
+__device__ __forceinline__ T shfl_val(T v, int src) {
+    if constexpr (sizeof(T) < 4) return (T)__shfl_sync(0xffffffffu, (int)v, src);
+    else return __shfl_sync(0xffffffffu, v, src);
+}
+
+constexpr int kSparseQueries = 8;  // items with at most this many points use candidate lanes
+constexpr int kMaxRanges = 32;     // neighbour ranges kept in shared memory (3^d <= 32: d <= 3)
+
 template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
-    const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
+    __shared__ int2 s_rng[4][kMaxRanges];
+    const int w = threadIdx.x >> 5;
+    const int item = blockIdx.x * 4 + w;
     if (item >= a.n_items) return;
     const Tile<T> tile = warp_tile<T>(a.g.d);
     const int2 it = a.items[item];
@@ -290,6 +320,61 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
     load_query<T, D>(a, p, active, q);
     int count = 0;
     const int limit = a.min_points;
+    if (a.dense_id) {
+        // a point of a dense cell whose sub-cell holds >= minPoints points has that many
+        // neighbours within eps already (sub-cells are certified cliques)
+        const int id = a.dense_id[r];
+        if (id >= 0 && active) {
+            const int g = a.dense_gidx[p];
+            const int* grp = a.dense_grp + (size_t)id * (a.dense_groups + 1);
+            if (grp[g + 1] - grp[g] >= limit) count = limit;
+        }
+        if (__all_sync(0xffffffffu, !active || count >= limit)) {
+            if (active) a.core[p] = 1;
+            return;
+        }
+    }
+    int S = 1;
+    for (int sd = 0; sd < a.g.d; ++sd) S *= 3;
+    if (pend - it.y <= kSparseQueries && S <= kMaxRanges) {
+        // few queries: the whole warp tests consecutive candidates of one query at a
+        // time (a ballot counts the hits), instead of leaving most lanes idle
+        int nr = 0;
+        visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
+            if (lane_id() == 0) s_rng[w][nr] = make_int2(a.ct.start[cr], a.ct.start[cr + 1]);
+            ++nr;
+            return true;
+        });
+        __syncwarp();
+        for (int src = 0; src < pend - it.y; ++src) {
+            T qq[D > 0 ? D : kMaxDims];
+#pragma unroll
+            for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                if (D == 0 && k >= a.g.d) break;
+                qq[k] = shfl_val(q[k], src);
+            }
+            int hits = 0;
+            for (int ri = 0; ri < nr && hits < limit; ++ri) {
+                const int ce = s_rng[w][ri].y;
+                for (int j0 = s_rng[w][ri].x; j0 < ce && hits < limit; j0 += 32) {
+                    const int j = j0 + (int)lane_id();
+                    bool hit = false;
+                    if (j < ce) {
+                        T c[D > 0 ? D : kMaxDims];
+#pragma unroll
+                        for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                            if (D == 0 && k >= a.g.d) break;
+                            c[k] = a.coords[(size_t)k * a.n + j];
+                        }
+                        hit = within_vals<T, M, D>(a, qq, c);
+                    }
+                    hits += __popc(__ballot_sync(0xffffffffu, hit));
+                }
+            }
+            if (lane_id() == 0) a.core[it.y + src] = hits >= limit ? 1 : 0;
+        }
+        return;
+    }
     auto aux_of = [](int) { return 0; };
     auto pair = [&](int, int u, int) {
         if (active && within<T, M, D>(a, q, tile, u)) ++count;
@@ -388,7 +473,8 @@ static __global__ void k_dense_list(const int32_t* cell_start, int m, DenseArgs 
     }
 }
 
-// block per dense cell: sub-cell of every point, counting sort into sec, star roots
+// block per dense cell: sub-cell of every point and a counting sort of the cell's
+// points by sub-cell into sec (runs before the core test, which uses the counts)
 template <typename T>
 __global__ void __launch_bounds__(256) k_dense_group(QueryArgs<T> a, DenseArgs da) {
     __shared__ int cnt[256];
@@ -397,10 +483,7 @@ __global__ void __launch_bounds__(256) k_dense_group(QueryArgs<T> a, DenseArgs d
     if (id >= *da.n_dense) return;
     const int c = da.cells[id];
     const int s0 = a.ct.start[c], s1 = a.ct.start[c + 1];
-    for (int g = threadIdx.x; g < da.groups; g += blockDim.x) {
-        cnt[g] = 0;
-        da.grp_rep[(size_t)id * da.groups + g] = INT_MAX;
-    }
+    for (int g = threadIdx.x; g < da.groups; g += blockDim.x) cnt[g] = 0;
     __syncthreads();
     for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
         int g = 0, mul = 1;
@@ -414,7 +497,6 @@ __global__ void __launch_bounds__(256) k_dense_group(QueryArgs<T> a, DenseArgs d
         }
         da.gidx[i] = g;
         atomicAdd(&cnt[g], 1);
-        if (a.core[i]) atomicMin(&da.grp_rep[(size_t)id * da.groups + g], i);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -430,11 +512,28 @@ __global__ void __launch_bounds__(256) k_dense_group(QueryArgs<T> a, DenseArgs d
     for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
         const int g = da.gidx[i];
         da.sec[s0 + atomicAdd(&cur[g], 1)] = i;
-        // star union inside the sub-cell: the smallest core is a root at this point
-        if (a.core[i]) {
-            const int rep = da.grp_rep[(size_t)id * da.groups + g];
-            if (rep != i) a.parent[i] = rep;
-        }
+    }
+}
+
+// block per dense cell: the smallest core of every sub-cell becomes the root of a star
+// over the sub-cell's cores (they are pairwise within eps); runs before any union
+template <typename T>
+__global__ void __launch_bounds__(256) k_dense_star(QueryArgs<T> a, DenseArgs da) {
+    __shared__ int rep[256];
+    const int id = blockIdx.x;
+    if (id >= *da.n_dense) return;
+    const int c = da.cells[id];
+    const int s0 = a.ct.start[c], s1 = a.ct.start[c + 1];
+    for (int g = threadIdx.x; g < da.groups; g += blockDim.x) rep[g] = INT_MAX;
+    __syncthreads();
+    for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x)
+        if (a.core[i]) atomicMin(&rep[da.gidx[i]], i);
+    __syncthreads();
+    for (int g = threadIdx.x; g < da.groups; g += blockDim.x) da.grp_rep[(size_t)id * da.groups + g] = rep[g];
+    for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+        if (!a.core[i]) continue;
+        const int r = rep[da.gidx[i]];
+        if (r != i) a.parent[i] = r;
     }
 }
 
