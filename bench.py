@@ -40,6 +40,14 @@ PROFILE = os.path.join(ROOT, "profiles", "k_core_blobs10m.txt")
 CROP = 0.10  # CPU sample: spatial crop of the workload (keeps its density)
 
 
+T0 = time.perf_counter()
+
+
+def progress(msg):
+    """Stage marks on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.perf_counter() - T0:7.1f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -199,7 +207,6 @@ def measure_served(duration_s, workers, rate=200.0):
     trace = workloads.serve_trace(seed=0, rate=rate, duration_s=duration_s)
     pools = {}
     for d in (2, 3, 4):
-        w = workloads.batch_instance(7000 + d, n_max=5_000_001)
         rng = np.random.default_rng(d)
         centres = rng.random((40, d))
         pools[d] = workloads._mixture(rng, 5_000_000, d, centres, np.exp(rng.uniform(np.log(0.005), np.log(0.05), 40)),
@@ -289,6 +296,7 @@ def run_engine(args):
         os.path.join(ROOT, "gpurun_out")) else f"/tmp/hpd_clocks_{os.getpid()}.csv")
     step_ms, core_ms, phases = [], [], []
     launches = 0
+    progress("device-resident steps")
     with clock:
         wall0 = time.perf_counter()
         for _ in range(args.steps):
@@ -314,6 +322,7 @@ def run_engine(args):
     value = world * n * args.steps / (total_ms / 1000) / 1e6
 
     # end to end through the host-buffer entry point (pinned input, labels back to host)
+    progress("host-buffer steps")
     pinned = torch.from_numpy(w.points).pin_memory()
     host_labels = torch.empty(n, dtype=torch.int64).pin_memory()
     import ctypes
@@ -351,11 +360,15 @@ def run_engine(args):
     from oracle import pyoracle
     pyoracle.build(ref=None)
     crop = cpu_sample(w.points, w.eps, w.min_points, CROP)
+    progress("CPU baseline")
     kind, threads, ts = time_cpu(crop, w.eps, w.min_points, 2)
     cpu_val = len(crop) / statistics.median(ts) / 1e6
     mean = lambda key: sum(p[key] for p in phases) / len(phases)
+    progress("batched jobs")
     batched = measure_batched(args.batch_instances, 8) if args.batch_instances > 0 else None
+    progress("served trace")
     served = measure_served(args.serve_seconds, 8) if args.serve_seconds > 0 else None
+    progress("done")
     line = {
         "metric": METRIC, "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",

@@ -16,8 +16,9 @@ HPD_ERR_GRID, HPD_ERR_NOMEM, HPD_ERR_CUDA, HPD_ERR_TIMEOUT = 4, 5, 6, 7
 F32, F64, I8, I16, I32, I64, U8, U16, U32, U64 = range(10)
 CELL_RECIP, CELL_DIV = 0, 1
 DIST_GCC_X86, DIST_SEQ, DIST_SEQ_FMA = 0, 1, 2
+TIE_EXACT, TIE_SMALLEST_ID = 0, 1
 
-EXPORTS = ("hpd_create", "hpd_destroy", "hpd_set_arith", "hpd_cluster", "hpd_cluster_device",
+EXPORTS = ("hpd_create", "hpd_destroy", "hpd_set_arith", "hpd_set_tie_break", "hpd_cluster", "hpd_cluster_device",
            "hpd_get_stats", "hpd_last_error", "hpd_version", "hpd_cluster_device_noalloc",
            "hpd_noalloc_last_error", "hpd_cluster_batch", "hpd_server_create", "hpd_server_submit",
            "hpd_server_poll", "hpd_server_wait", "hpd_server_destroy", "hpd_server_last_error")
@@ -65,6 +66,8 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.hpd_destroy.restype = None
     lib.hpd_set_arith.argtypes = [H, ctypes.c_int, ctypes.c_int]
     lib.hpd_set_arith.restype = ctypes.c_int
+    lib.hpd_set_tie_break.argtypes = [H, ctypes.c_int]
+    lib.hpd_set_tie_break.restype = ctypes.c_int
     lib.hpd_cluster.argtypes = [H, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                 ctypes.c_void_p]
     lib.hpd_cluster.restype = ctypes.c_int

@@ -16,6 +16,7 @@ struct hpd_handle {
     uint64_t min_points;
     int cell_mode = HPD_CELL_RECIP;
     int dist_mode = HPD_DIST_GCC_X86;
+    int tie_mode = HPD_TIE_EXACT;
     int device = 0;
     cudaStream_t stream = nullptr;
     Arena small, main, in_buf, out_buf;
@@ -60,6 +61,7 @@ int run(hpd_handle* h, const void* d_data, int64_t n, int32_t d, int32_t dtype, 
     rq.min_points = h->min_points;
     rq.cell_mode = h->cell_mode;
     rq.dist_mode = h->dist_mode;
+    rq.tie_mode = h->tie_mode;
     rq.d_labels = d_labels;
     rq.stream = s;
     std::string err;
@@ -129,6 +131,13 @@ int hpd_set_arith(hpd_handle* h, int cell_mode, int dist_mode) {
     if (dist_mode < HPD_DIST_GCC_X86 || dist_mode > HPD_DIST_SEQ_FMA) return fail(HPD_ERR_INVALID, "bad distance mode");
     h->cell_mode = cell_mode;
     h->dist_mode = dist_mode;
+    return HPD_OK;
+}
+
+int hpd_set_tie_break(hpd_handle* h, int mode) {
+    if (!h) return fail(HPD_ERR_INVALID, "null handle");
+    if (mode != HPD_TIE_EXACT && mode != HPD_TIE_SMALLEST_ID) return fail(HPD_ERR_INVALID, "bad tie-break mode");
+    h->tie_mode = mode;
     return HPD_OK;
 }
 

@@ -57,6 +57,7 @@ struct Request {
     uint64_t min_points;
     int cell_mode;
     int dist_mode;
+    int tie_mode = 0;    // 0: exact reference tie-break; 1: smallest cluster id
     int64_t* d_labels;   // device, input order
     cudaStream_t stream;
     bool no_dense = false;  // look cells up by binary search only (no grid-sized table)

@@ -229,11 +229,13 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     uint32_t* counts = main.take<uint32_t>(ncounts);
     uint32_t* scan32 = main.take<uint32_t>(2 * nscan);
     uint32_t* totals = main.take<uint32_t>(4);   // cells, items
-    int* flags_dev = main.take<int>(16);          // list counters, diagnostics
+    int* flags_dev = main.take<int>(16);          // list counters, [6] cores, diagnostics, [13..15] range-check record
     if (main.overflowed()) {
         err = "internal error: device buffer plan exceeds its reservation";
         return kRuntime;
     }
+    int* guard = flags_dev + 13;
+    HPD_CU(cudaMemsetAsync(flags_dev, 0, 16 * sizeof(int), s));
 
     // ---- cell ids (spatial_index.h:144-165)
     CellParams cp;
@@ -285,6 +287,8 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     a.ct.m = m;
     a.ct.ccoord = ccoord;
     a.ct.pitch = n;
+    a.ct.guard = guard;
+    a.guard = guard;
     a.eps2 = eps2_of<T>(rq.eps);  // const float EPS2 = eps * eps (hpdbscan.h:53), converted to T
     a.items = items;
     a.n_items = n_items;
@@ -355,22 +359,29 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     k_cell_rep<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep);
     k_cell_uniform<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep, cell_flags);
     HPD_QUERY_DISPATCH(k_union_cross, T, mode, d, qgrid, 128, qsmem, s, a);
-    k_compress<<<blocks_for(n, 256), 256, 0, s>>>(parent, core, n);
+    k_compress<<<blocks_for(n, 256), 256, 0, s>>>(parent, core, n, flags_dev + 6);
     info.launches += 7;
     if (timed) HPD_CU(cudaEventRecord(tm->ev[3], s));
 
     // ---- borders
-    HPD_CU(cudaMemsetAsync(flags_dev, 0, 8 * sizeof(int), s));
+    HPD_CU(cudaMemsetAsync(flags_dev, 0, 6 * sizeof(int), s));
     HPD_QUERY_DISPATCH(k_border, T, mode, d, qgrid, 128, qsmem, s, a);
     info.launches += 1;
-    int h_amb = 0;
-    HPD_CU(cudaMemcpyAsync(&h_amb, flags_dev, sizeof(int), cudaMemcpyDeviceToHost, s));
+    int h_counts[7];  // [0] ambiguous borders, [6] cores
+    HPD_CU(cudaMemcpyAsync(h_counts, flags_dev, sizeof h_counts, cudaMemcpyDeviceToHost, s));
     HPD_CU(cudaStreamSynchronize(s));
+    const int h_amb = h_counts[0];
     info.n_ambiguous = h_amb;
+    info.n_core = h_counts[6];
     if (timed) HPD_CU(cudaEventRecord(tm->ev[4], s));
 
     // ---- tie-break for borders next to several clusters
-    if (h_amb > 0) {
+    if (h_amb > 0 && rq.tie_mode != 0) {
+        a.amb = amb;
+        a.n_amb = flags_dev + 0;
+        HPD_QUERY_DISPATCH(k_tie_min_root, T, mode, d, blocks_for(h_amb, 4), 128, 0, s, a);
+        info.launches += 1;
+    } else if (h_amb > 0) {
         const bool trace = getenv("HPD_TIE_TRACE") != nullptr;
         unsigned long long* tcount = reinterpret_cast<unsigned long long*>(flags_dev + 8);
         a.trace_counts = trace ? tcount : nullptr;
@@ -457,7 +468,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 k_tie_schedule<T><<<list_grid, 128, 0, s>>>(a);
                 exclusive_scan<uint32_t>(item_flag, item_pos, n_items, scan32,
                                          reinterpret_cast<uint32_t*>(a.n_wlist_out), s, &info.launches);
-                k_tie_compact<<<blocks_for(n_items, 256), 256, 0, s>>>(item_flag, item_pos, n_items, a.wlist_out);
+                k_tie_compact<<<blocks_for(n_items, 256), 256, 0, s>>>(item_flag, item_pos, n_items, a.wlist_out, guard);
                 info.launches += 4;
                 if (trace) {
                     unsigned long long tc[2];
@@ -501,8 +512,15 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     k_finalize<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, broot, perm, n, rq.d_labels);
     info.launches += 1;
     if (timed) HPD_CU(cudaEventRecord(tm->ev[6], s));
+    int h_guard[3] = {0, 0, 0};
+    HPD_CU(cudaMemcpyAsync(h_guard, guard, sizeof h_guard, cudaMemcpyDeviceToHost, s));
     HPD_CU(cudaGetLastError());
     HPD_CU(cudaStreamSynchronize(s));
+    if (h_guard[0]) {
+        err = "internal error: device index out of range (check " + std::to_string(h_guard[1]) + ", index " +
+              std::to_string(h_guard[2]) + ", " + std::to_string(h_guard[0]) + " times)";
+        return kRuntime;
+    }
     if (timed) {
         float ms = 0;
         cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[6]); info.ms[0] = ms;

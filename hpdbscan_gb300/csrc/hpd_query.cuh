@@ -17,6 +17,22 @@
 
 namespace hpd {
 
+// Range check of an index read from device tables: an index outside [0, bound) is
+// recorded in guard[0..2] (count, tag, index) and the access is skipped, so that a
+// corrupted table ends the call with an error status instead of a memory fault.
+enum GuardTag : int {
+    kGuardStencilKey = 1, kGuardStencilCell, kGuardItem, kGuardRoot, kGuardDirtyCell, kGuardDirtyList,
+    kGuardAmbiguous, kGuardLabel, kGuardCellRank, kGuardItemIndex, kGuardList, kGuardCount
+};
+__device__ __forceinline__ bool in_range(int* guard, long long i, long long bound, int tag) {
+    if (i >= 0 && i < bound) return true;
+    if (guard && atomicAdd(guard, 1) == 0) {
+        guard[1] = tag;
+        guard[2] = (int)i;
+    }
+    return false;
+}
+
 struct CellTable {
     const int32_t* start;              // [m + 1] first sorted position of each cell
     const unsigned long long* key;     // [m] cell id
@@ -24,6 +40,7 @@ struct CellTable {
     const uint32_t* ccoord;            // [d][pitch] grid coordinate of each cell, swapped order
     int m;
     int pitch;
+    int* guard;                        // range-check record (see in_range)
 };
 
 __device__ __forceinline__ int find_cell(const CellTable& ct, unsigned long long key) {
@@ -71,7 +88,11 @@ __device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct
                     if (coord[s] + 1 >= g.dims[g.swapped[s]]) ok = false; else nk += g.stride[s];
                 }
             }
-            if (ok && (sel == 0 || (sel == 1 ? nk < key : nk > key))) nr = find_cell(ct, nk);
+            if (ok && (sel == 0 || (sel == 1 ? nk < key : nk > key))) {
+                nr = (ct.dense && !in_range(ct.guard, (long long)nk, (long long)g.total, kGuardStencilKey))
+                         ? -1 : find_cell(ct, nk);
+                if (nr >= 0 && !in_range(ct.guard, nr, ct.m, kGuardStencilCell)) nr = -1;
+            }
             // the per-cell filter runs on all lanes at once, hiding its load latency
             if (nr >= 0 && !keep(nr)) nr = -1;
         }
@@ -144,6 +165,7 @@ struct QueryArgs {
     uint32_t* item_flag;  // items scheduled for the next pass
     int* ticket;          // next work-list entry to take
     unsigned long long* trace_counts;  // diagnostics (nullptr: off): [0] active lanes, [1] tiles scanned
+    int* guard;           // range-check record (see in_range)
     const int* dense_id;  // per cell: >= 0 when the dense-cell kernels connect its cores
     const int* dense_grp; // [dense][groups + 1] sub-cell starts (see DenseArgs)
     const int* dense_gidx;  // per point of a dense cell: its sub-cell
@@ -163,6 +185,14 @@ struct Tile {
     T* c;      // [32][tile_stride(d)]
     int* aux;  // [32]
 };
+
+// tmax of the component of a cell's representative core (range-checked)
+template <typename T>
+__device__ __forceinline__ int tmax_of(const QueryArgs<T>& a, int rep_c) {
+    if (!in_range(a.guard, rep_c, a.n, kGuardRoot)) return INT_MAX;
+    const int root = a.parent[rep_c];
+    return in_range(a.guard, root, a.n, kGuardRoot) ? a.tmax[root] : INT_MAX;
+}
 
 template <typename T>
 __device__ __forceinline__ Tile<T> warp_tile(int d) {
@@ -638,9 +668,13 @@ __global__ void __launch_bounds__(128) k_union_cross(QueryArgs<T> a) {
     }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore; });
 }
 
-static __global__ void k_compress(int* parent, const uint8_t* core, int n) {
+// every core points at its component root; counts the cores (one atomic per warp)
+static __global__ void k_compress(int* parent, const uint8_t* core, int n, int* n_core) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && core[i]) parent[i] = uf_find(parent, i);
+    const bool c = i < n && core[i];
+    if (c) parent[i] = uf_find(parent, i);
+    const unsigned m = __ballot_sync(0xffffffffu, c);
+    if (lane_id() == 0 && m) atomicAdd(n_core, __popc(m));
 }
 
 // ---------------------------------------------------------- border assignment
@@ -746,7 +780,22 @@ template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_tie_mark(QueryArgs<T> a) {
     const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (w >= *a.n_amb) return;
-    scan_point<T, M, D>(a, a.amb[w], [&](int j) { atomicMax(a.tmax + a.parent[j], j); });
+    const int b = a.amb[w];
+    if (!in_range(a.guard, b, a.n, kGuardAmbiguous)) return;
+    scan_point<T, M, D>(a, b, [&](int j) {
+        if (in_range(a.guard, a.parent[j], a.n, kGuardRoot)) atomicMax(a.tmax + a.parent[j], j);
+    });
+}
+
+// Smallest-id tie-break: an ambiguous border takes the smallest root (cluster id)
+// among all its core eps-neighbours (k_border stops at the second cluster found).
+template <typename T, int M, int D>
+__global__ void __launch_bounds__(128) k_tie_min_root(QueryArgs<T> a) {
+    const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (w >= *a.n_amb) return;
+    const int p = a.amb[w];
+    if (!in_range(a.guard, p, a.n, kGuardAmbiguous)) return;
+    scan_point<T, M, D>(a, p, [&](int j) { atomicMin(a.broot + p, a.parent[j]); });
 }
 
 static __global__ void k_tie_init(const uint8_t* core, int* lm1, int n) {
@@ -756,7 +805,11 @@ static __global__ void k_tie_init(const uint8_t* core, int* lm1, int n) {
 
 template <typename T>
 __device__ __forceinline__ void mark_dirty_cell(const QueryArgs<T>& a, int c) {
-    if (atomicMax(a.dirty_gen + c, a.gen) < a.gen) a.dlist[atomicAdd(a.n_dlist, 1)] = c;
+    if (!in_range(a.guard, c, a.ct.m, kGuardDirtyCell)) return;
+    if (atomicMax(a.dirty_gen + c, a.gen) < a.gen) {
+        const int k = atomicAdd(a.n_dlist, 1);
+        if (in_range(a.guard, k, a.ct.m, kGuardDirtyList)) a.dlist[k] = c;
+    }
 }
 
 // One relaxation pass over decreasing core edges for one work item.  Only
@@ -767,13 +820,16 @@ __device__ __forceinline__ void mark_dirty_cell(const QueryArgs<T>& a, int c) {
 // improvements inside one chunk settle within this pass.
 template <typename T, int M, int D>
 __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
+    if (!in_range(a.guard, item, a.n_items, kGuardItem)) return;
     const int2 it = a.items[item];
     const int r = it.x;
+    if (!in_range(a.guard, r, a.ct.m, kGuardCellRank) || !in_range(a.guard, it.y, a.n, kGuardItem)) return;
     const int pend = min(it.y + 32, a.ct.start[r + 1]);
     const int p = it.y + (int)lane_id();
     bool active = p < pend && a.core[p];
     const int root = active ? a.parent[p] : INT_MIN;
     // a core whose value is its component root holds the smallest value possible
+    if (active && !in_range(a.guard, root, a.n, kGuardRoot)) active = false;
     if (active) active = p <= a.tmax[root] && ld_volatile(a.lm1 + p) > root;
     if (!__any_sync(0xffffffffu, active)) return;
     if (a.trace_counts) {
@@ -811,6 +867,7 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
         const int first_item = (int)a.ipos[a.ct.start[cr]];
         for (int t0 = cs; t0 < ce; t0 += 32) {
             const int ti = first_item + ((t0 - a.ct.start[cr]) >> 5);
+            if (!in_range(a.guard, ti, a.n_items, kGuardItemIndex)) return false;
             if (ld_volatile(a.item_min_l + ti) >= worst) continue;
             if (a.trace_counts && lane_id() == 0) atomicAdd(a.trace_counts + 1, 1ull);
             if (scan_range(a, tile, t0, min(t0 + 32, ce), aux_of, pair, settled)) return true;
@@ -845,7 +902,7 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
         if (ld_volatile(a.dirty_gen + cr) < since) return true;
         const int rep_c = a.cell_rep[cr];
         if (rep_c == kNoCore) return true;
-        if ((a.cell_flags[cr] & kCellUniform) && a.tmax[a.parent[rep_c]] < a.ct.start[cr]) return true;
+        if ((a.cell_flags[cr] & kCellUniform) && tmax_of(a, rep_c) < a.ct.start[cr]) return true;
         // no core of that cell holds a value below any lane's: nothing to gain
         if (settled()) return true;
         int worst = (active && myl > root) ? myl : INT_MIN;
@@ -858,7 +915,7 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
         if (ld_volatile(a.dirty_gen + cr) < since) return false;
         const int rep_c = a.cell_rep[cr];
         if (rep_c == kNoCore) return false;
-        if ((a.cell_flags[cr] & kCellUniform) && a.tmax[a.parent[rep_c]] < a.ct.start[cr]) return false;
+        if ((a.cell_flags[cr] & kCellUniform) && tmax_of(a, rep_c) < a.ct.start[cr]) return false;
         return ld_volatile(a.cell_min_l + cr) < worst0;
     });
     if (__any_sync(0xffffffffu, active && myl < start_l) && lane_id() == 0) mark_dirty_cell(a, r);
@@ -875,7 +932,8 @@ __global__ void __launch_bounds__(128) k_tie_edge(QueryArgs<T> a) {
 // fixed grid of warps that take the next item from a shared ticket.
 template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_tie_edge_list(QueryArgs<T> a) {
-    const int cnt = *a.n_wlist;
+    int cnt = *a.n_wlist;
+    if (!in_range(a.guard, cnt, (long long)a.n_items + 1, kGuardCount)) cnt = 0;
     for (;;) {
         int wi = 0;
         if (lane_id() == 0) wi = atomicAdd(a.ticket, 1);
@@ -894,6 +952,7 @@ __global__ void k_tie_jump(QueryArgs<T> a) {
     if (l == INT_MAX || l == i) return;
     const int l0 = l;
     for (;;) {  // strictly decreasing, so at most n steps
+        if (!in_range(a.guard, l, a.n, kGuardLabel)) return;
         const int ll = ld_volatile(a.lm1 + l);
         if (ll >= l) break;
         l = ll;
@@ -901,9 +960,12 @@ __global__ void k_tie_jump(QueryArgs<T> a) {
     if (l < l0) {
         atomicMin(a.lm1 + i, l);
         const int c = (int)a.cellrank[i];
+        if (!in_range(a.guard, c, a.ct.m, kGuardCellRank)) return;
         atomicMin(a.cell_min_l + c, l);
         const int s0 = a.ct.start[c];
-        atomicMin(a.item_min_l + (int)a.ipos[s0] + ((i - s0) >> 5), l);
+        const int ti = (int)a.ipos[s0] + ((i - s0) >> 5);
+        if (!in_range(a.guard, ti, a.n_items, kGuardItemIndex)) return;
+        atomicMin(a.item_min_l + ti, l);
         if (a.gen > 0) mark_dirty_cell(a, c);
     }
 }
@@ -914,9 +976,12 @@ __global__ void k_tie_cell_min(QueryArgs<T> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n || !a.core[i]) return;
     const int c = (int)a.cellrank[i];
+    if (!in_range(a.guard, c, a.ct.m, kGuardCellRank)) return;
     atomicMin(a.cell_min_l + c, a.lm1[i]);
     const int s0 = a.ct.start[c];
-    atomicMin(a.item_min_l + (int)a.ipos[s0] + ((i - s0) >> 5), a.lm1[i]);
+    const int ti = (int)a.ipos[s0] + ((i - s0) >> 5);
+    if (!in_range(a.guard, ti, a.n_items, kGuardItemIndex)) return;
+    atomicMin(a.item_min_l + ti, a.lm1[i]);
 }
 
 // Next pass's work: the items of every cell whose lower stencil or own cell was
@@ -925,36 +990,39 @@ __global__ void k_tie_cell_min(QueryArgs<T> a) {
 template <typename T>
 __global__ void __launch_bounds__(128) k_tie_schedule(QueryArgs<T> a) {
     const int nw = gridDim.x * 4;
-    const int cnt = *a.n_dlist;
+    int cnt = *a.n_dlist;
+    if (!in_range(a.guard, cnt, (long long)a.ct.m + 1, kGuardCount)) cnt = 0;
     const unsigned lane = lane_id();
     for (int w = blockIdx.x * 4 + (threadIdx.x >> 5); w < cnt; w += nw) {
         const int c = a.dlist[w];
+        if (!in_range(a.guard, c, a.ct.m, kGuardDirtyCell)) continue;
         visit_stencil(a.g, a.ct, c, 2, [&](int cr, bool) {
             const int rep_c = a.cell_rep[cr];
             if (rep_c == kNoCore) return true;
-            if ((a.cell_flags[cr] & kCellUniform) && a.tmax[a.parent[rep_c]] < a.ct.start[cr]) return true;
+            if ((a.cell_flags[cr] & kCellUniform) && tmax_of(a, rep_c) < a.ct.start[cr]) return true;
             int fresh = 0;
             if (lane == 0) fresh = atomicMax(a.sched_gen + cr, a.gen) < a.gen;
             if (!__shfl_sync(0xffffffffu, fresh, 0)) return true;
             const int s0 = a.ct.start[cr];
             const int nit = (a.ct.start[cr + 1] - s0 + 31) >> 5;
             const int first = (int)a.ipos[s0];
-            for (int k = (int)lane; k < nit; k += 32) a.item_flag[first + k] = 1u;
+            for (int k = (int)lane; k < nit; k += 32)
+                if (in_range(a.guard, first + k, a.n_items, kGuardItemIndex)) a.item_flag[first + k] = 1u;
             return true;
         }, false, [&](int cr) {
             const int rep_c = a.cell_rep[cr];
             if (rep_c == kNoCore) return false;
-            return !((a.cell_flags[cr] & kCellUniform) && a.tmax[a.parent[rep_c]] < a.ct.start[cr]);
+            return !((a.cell_flags[cr] & kCellUniform) && tmax_of(a, rep_c) < a.ct.start[cr]);
         });
     }
 }
 
 // Lists the flagged items in increasing order (pos = exclusive scan of the flags)
 // and clears the flags for the next pass.
-static __global__ void k_tie_compact(uint32_t* item_flag, const uint32_t* pos, int n_items, int* wlist) {
+static __global__ void k_tie_compact(uint32_t* item_flag, const uint32_t* pos, int n_items, int* wlist, int* guard) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n_items && item_flag[i]) {
-        wlist[pos[i]] = i;
+        if (in_range(guard, pos[i], n_items, kGuardList)) wlist[pos[i]] = i;
         item_flag[i] = 0u;
     }
 }
@@ -1014,6 +1082,7 @@ __global__ void __launch_bounds__(128) k_tie_decide(QueryArgs<T> a, int final_pa
     const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (w >= *a.n_amb) return;
     const int b = a.amb[w];
+    if (!in_range(a.guard, b, a.n, kGuardAmbiguous)) return;
     unsigned long long best = ~0ull;  // (upper bound of L - 1) << 32 | root
     scan_point<T, M, D>(a, b, [&](int j) {
         const unsigned long long v = ((unsigned long long)(unsigned)ld_volatile(a.lm1 + j) << 32) | (unsigned)a.parent[j];

@@ -51,6 +51,12 @@ class HPDBSCAN:
     def set_arith(self, cell_mode: int = _lib.CELL_RECIP, dist_mode: int = _lib.DIST_GCC_X86) -> None:
         _lib.raise_for(self._lib.hpd_set_arith(self._h, cell_mode, dist_mode))
 
+    def set_tie_break(self, mode: int = _lib.TIE_EXACT) -> None:
+        """TIE_EXACT (default): the single-thread reference's labels.  TIE_SMALLEST_ID:
+        borders next to several clusters take the smallest cluster id among their core
+        neighbours (faster; cores, noise and other borders unchanged)."""
+        _lib.raise_for(self._lib.hpd_set_tie_break(self._h, mode))
+
     def cluster(self, data, dataset: str | None = None, threads: int | None = None):
         """cluster(ndarray) | cluster(path, dataset[, threads]) -> tuple of int."""
         if isinstance(data, (str, bytes)):

@@ -100,6 +100,11 @@ public:
     void set_arith(int cell_mode, int dist_mode) {
         hpdbscan_gb300_detail::raise(hpd_set_arith(m_handle, cell_mode, dist_mode));
     }
+
+    /* HPD_TIE_EXACT (default) or HPD_TIE_SMALLEST_ID (see hpdbscan_gb300.h) */
+    void set_tie_break(int mode) {
+        hpdbscan_gb300_detail::raise(hpd_set_tie_break(m_handle, mode));
+    }
 };
 
 #endif

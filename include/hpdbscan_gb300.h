@@ -88,6 +88,16 @@ void hpd_destroy(hpd_handle* h);
 
 int hpd_set_arith(hpd_handle* h, int cell_mode, int dist_mode);
 
+/* Labels of border points next to two or more clusters.  HPD_TIE_EXACT (default)
+ * gives the label the single-thread reference gives (the smallest provisional label
+ * offered while its loop runs, hpdbscan.h:72-92), which needs a relaxation over
+ * the provisional labels of the cores.  HPD_TIE_SMALLEST_ID skips it and gives such a
+ * border the smallest cluster id among its core neighbours: a valid DBSCAN result
+ * (the multi-threaded reference may give either), and cores, noise and every other
+ * border keep their exact labels.  No counterpart in the reference. */
+typedef enum { HPD_TIE_EXACT = 0, HPD_TIE_SMALLEST_ID = 1 } hpd_tie_mode;
+int hpd_set_tie_break(hpd_handle* h, int mode);
+
 /* Labels for n points of d coordinates (row-major, host memory) into labels[n]
  * (host memory), in input order.  `threads` is accepted for interface parity and
  * unused: the work runs on the current CUDA device. */

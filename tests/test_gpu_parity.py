@@ -95,3 +95,52 @@ def test_gpu_input_not_modified(gpu):
     before = pts.copy()
     engine(0.02, 8).cluster_array(pts)
     assert np.array_equal(pts, before)
+
+
+def _smallest_root_labels(points, eps, exact):
+    """Expected smallest-id labels from the exact ones: a border takes 1 + the
+    smallest root among its core eps-neighbours (float32 d = 3: the squared distance
+    is the sequential float sum, as in the engine's default arithmetic)."""
+    from scipy.spatial import cKDTree
+    eps2 = np.float32(eps) * np.float32(eps)
+    core = np.flatnonzero(exact < 0)
+    tree = cKDTree(points[core].astype(np.float64))
+    want = exact.copy()
+    border = np.flatnonzero(exact > 0)
+    for b, cand in zip(border, tree.query_ball_point(points[border].astype(np.float64), float(eps) * 1.001)):
+        c = core[np.asarray(cand, dtype=np.int64)]
+        t = points[c] - points[b]
+        sq = (t[:, 0] * t[:, 0] + t[:, 1] * t[:, 1]) + t[:, 2] * t[:, 2]
+        roots = -exact[c[sq <= eps2]] - 1
+        want[b] = roots.min() + 1
+    return want
+
+
+def test_gpu_smallest_id_tie_break(gpu):
+    """HPD_TIE_SMALLEST_ID: cores, noise and single-cluster borders keep their exact
+    labels; a border next to several clusters takes the smallest of their ids."""
+    from hpdbscan_gb300 import _lib, workloads
+    w = workloads.blobs_10m(seed=0, n=300_000)
+    exact = engine(w.eps, w.min_points).cluster_array(w.points)
+    h = engine(w.eps, w.min_points)
+    h.set_tie_break(_lib.TIE_SMALLEST_ID)
+    fast = h.cluster_array(w.points)
+    assert h.stats()["n_ambiguous"] > 0
+    assert np.array_equal(fast[exact <= 0], exact[exact <= 0])
+    assert np.array_equal(fast == 0, exact == 0)
+    assert np.array_equal(fast, _smallest_root_labels(w.points, w.eps, exact))
+    h.set_tie_break(_lib.TIE_EXACT)
+    assert np.array_equal(h.cluster_array(w.points), exact)
+    with pytest.raises(ValueError):
+        h.set_tie_break(7)
+
+
+def test_gpu_stats_counts(gpu, oracle):
+    """hpd_get_stats: cores and cells of the last call match the labels and the grid."""
+    pts, eps, mp, labels = load_golden("blobs100k_s0")
+    h = engine(eps, mp)
+    assert np.array_equal(h.cluster_array(pts), labels)
+    st = h.stats()
+    assert st["n_core"] == int((labels < 0).sum())
+    _, _, cells = oracle.cluster(pts, eps, mp, with_order=True)
+    assert st["n_cells"] == len(np.unique(cells))
