@@ -219,12 +219,20 @@ __global__ void k_cell_table(const K* __restrict__ keys, int64_t n, const uint32
 
 // Work items of the query kernels: chunks of up to 32 consecutive points of one
 // cell.  item_flag[i] = 1 where a chunk starts.
+// Also records the largest cell population in *max_cell (one atomic per warp).
 static __global__ void k_item_flags(const uint32_t* __restrict__ cellrank, const int32_t* __restrict__ cell_start, int64_t n,
-                             uint32_t* __restrict__ item_flag) {
+                             uint32_t* __restrict__ item_flag, uint32_t* __restrict__ max_cell) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int32_t s = cell_start[cellrank[i]];
-    item_flag[i] = ((i - s) & 31) == 0 ? 1u : 0u;
+    uint32_t v = 0;
+    if (i < n) {
+        const uint32_t c = cellrank[i];
+        const int32_t s = cell_start[c];
+        item_flag[i] = ((i - s) & 31) == 0 ? 1u : 0u;
+        if (s == (int32_t)i) v = (uint32_t)(cell_start[c + 1] - s);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v) atomicMax(max_cell, v);
 }
 
 static __global__ void k_item_write(const uint32_t* __restrict__ item_flag, const uint32_t* __restrict__ item_pos,

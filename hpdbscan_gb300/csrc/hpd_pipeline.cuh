@@ -53,7 +53,29 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
         }                                                                                                    \
     } while (0)
 
+// Same, for kernels with a trailing bool template parameter B.
+#define HPD_QUERY_DISPATCH_B(KERNEL, B, T, mode, d, grid, block, smem, stream, ...)                                 \
+    do {                                                                                                     \
+        if constexpr (!Elem<T>::kFloat) {                                                                    \
+            /* integer sums wrap, so every summation order gives the same result */                          \
+            if ((d) == 2) KERNEL<T, kDistSeq, 2, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                \
+            else if ((d) == 3) KERNEL<T, kDistSeq, 3, B><<<grid, block, smem, stream>>>(__VA_ARGS__);           \
+            else KERNEL<T, kDistSeq, 0, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
+        } else if ((d) == 2) {                                                                               \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 2, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else KERNEL<T, kDistSeq, 2, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
+        } else if ((d) == 3) {                                                                               \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 3, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else KERNEL<T, kDistSeq, 3, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
+        } else {                                                                                             \
+            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 0, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else if ((mode) == kDistSeq) KERNEL<T, kDistSeq, 0, B><<<grid, block, smem, stream>>>(__VA_ARGS__);  \
+            else KERNEL<T, kDistGccX86, 0, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                      \
+        }                                                                                                    \
+    } while (0)
+
 constexpr int kDenseMinPoints = 128;  // cells with this many points take the dense-cell path
+constexpr int kFineMinPoints = 65536;  // a largest cell this big selects the finer sub-cell split
 
 template <typename T, typename K>
 int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, std::string& err, const Grid& g,
@@ -166,9 +188,10 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     need += (size_t)n + 5 * (size_t)n * 4;                           // core, tmax, parent, broot, lm1, amb
     need += (size_t)n * 4 + (size_t)n;                               // cell rep, cell flags
     need += 9 * (size_t)n * 4;                                       // dirty / schedule stamps, dirty list, work lists, cell / item min, item flags
-    // dense cells: sub-cells per dimension (0: path off), see k_dense_group
+    // dense cells: sub-cells per dimension (0: path off), see k_dense_assign
     int dense_k = 0;
-    if (Elem<T>::kFloat && d <= 4) {
+    // (squared distances near the float subnormal range would void the rounding margins)
+    if (Elem<T>::kFloat && d <= 4 && (double)rq.eps * (double)rq.eps >= 1e-30) {
         double err = 0;
         for (int k = 0; k < d; ++k)
             err = std::max(err, (std::fabs((double)mins[k]) + (double)g.dims[k] * (double)rq.eps) * std::ldexp(1.0, -20));
@@ -179,10 +202,18 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 dense_k = kk;
         }
     }
-    int dense_groups = 1;
-    for (int k = 0; k < d; ++k) dense_groups *= std::max(dense_k, 1);
+    // a grid whose largest cell holds >= kFineMinPoints points splits dense cells finer
+    // (decided once the cell table exists); the tables are sized for either split
+    const int fine_k = dense_k == 0 ? 0 : std::max(dense_k, d == 1 ? 32 : d == 2 ? 8 : d == 3 ? 4 : 3);
+    int dense_groups = 1, groups_cap = 1;
+    for (int k = 0; k < d; ++k) {
+        dense_groups *= std::max(dense_k, 1);
+        groups_cap *= std::max(fine_k, 1);
+    }
     const int64_t dense_max = (int64_t)n / kDenseMinPoints + 1;
-    need += 3 * (size_t)n * 4 + (size_t)dense_max * (2 * dense_groups + 2) * 4;  // dense-cell tables
+    need += 3 * (size_t)n * 4 + (size_t)dense_max * (3 * groups_cap + 2) * 4;  // dense-cell tables
+    need += dense_k ? (size_t)dense_max * groups_cap * 2 * d * sizeof(T) : 0;   // sub-cell boxes
+    need += dense_k ? (size_t)n * d * sizeof(T) : 0;                 // dense cells' coordinates by sub-cell
     need += (size_t)n * 4;                                           // second ambiguous list
     need += (size_t)ncounts * 4 + (size_t)nscan * 8 + 64;
     need += 64 * 256;                                                // alignment of up to 64 blocks
@@ -221,14 +252,17 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     uint32_t* item_flag = main.take<uint32_t>(n);
     int* dense_id = main.take<int>(n);
     int* dense_cells = main.take<int>(dense_max);
-    int* dense_grp = main.take<int>((size_t)dense_max * (dense_groups + 1));
-    int* dense_rep = main.take<int>((size_t)dense_max * dense_groups);
+    int* dense_grp = main.take<int>((size_t)dense_max * (groups_cap + 1));
+    int* dense_rep = main.take<int>((size_t)dense_max * groups_cap);
+    int* dense_cur = main.take<int>((size_t)dense_max * groups_cap);
     int* dense_sec = main.take<int>(n);
     int* dense_gidx = main.take<int>(n);
+    T* dense_box = main.take<T>(dense_k ? (size_t)dense_max * groups_cap * 2 * d : 0);
+    T* dense_coords = main.take<T>(dense_k ? (size_t)n * d : 0);
     uint32_t* item_pos = main.take<uint32_t>(n);
     uint32_t* counts = main.take<uint32_t>(ncounts);
     uint32_t* scan32 = main.take<uint32_t>(2 * nscan);
-    uint32_t* totals = main.take<uint32_t>(4);   // cells, items
+    uint32_t* totals = main.take<uint32_t>(4);   // cells, items, largest cell
     int* flags_dev = main.take<int>(16);          // list counters, [6] cores, diagnostics, [13..15] range-check record
     if (main.overflowed()) {
         err = "internal error: device buffer plan exceeds its reservation";
@@ -264,15 +298,20 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     k_cell_flags<K><<<blocks_for(n, 256), 256, 0, s>>>(skeys, n, flag);
     exclusive_scan<uint32_t>(flag, rank, n, scan32, totals + 0, s, &info.launches);
     k_cell_table<K><<<blocks_for(n, 256), 256, 0, s>>>(skeys, n, flag, rank, cell_start, cell_key, dense, ccoord, g);
-    k_item_flags<<<blocks_for(n, 256), 256, 0, s>>>(rank, cell_start, n, iflag);
+    HPD_CU(cudaMemsetAsync(totals + 2, 0, sizeof(uint32_t), s));
+    k_item_flags<<<blocks_for(n, 256), 256, 0, s>>>(rank, cell_start, n, iflag, totals + 2);
     exclusive_scan<uint32_t>(iflag, ipos, n, scan32, totals + 1, s, &info.launches);
     k_item_write<<<blocks_for(n, 256), 256, 0, s>>>(iflag, ipos, rank, n, items);
     info.launches += 5;
-    uint32_t h_tot[2];
-    HPD_CU(cudaMemcpyAsync(h_tot, totals, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    uint32_t h_tot[3];
+    HPD_CU(cudaMemcpyAsync(h_tot, totals, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     HPD_CU(cudaStreamSynchronize(s));
     const int m = (int)h_tot[0];
     const int n_items = (int)h_tot[1];
+    if (dense_k > 0 && h_tot[2] >= (uint32_t)kFineMinPoints) {
+        dense_k = fine_k;
+        dense_groups = groups_cap;
+    }
     info.n_cells = m;
     if (timed) HPD_CU(cudaEventRecord(tm->ev[1], s));
 
@@ -309,6 +348,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     const size_t qsmem = 4 * ((size_t)tile_stride(d) * 32 * sizeof(T) + 32 * sizeof(int));
 
     // ---- dense cells: sub-cells (certified cliques) for the core test and the unions
+    HPD_CU(cudaMemsetAsync(cell_flags, kCellUniform, m, s));
     DenseArgs da;
     memset(&da, 0, sizeof da);
     if (dense_k > 0) {
@@ -325,14 +365,25 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         da.grp_rep = dense_rep;
         da.sec = dense_sec;
         da.gidx = dense_gidx;
+        da.box = dense_box;
+        da.coords = dense_coords;
+        da.cur = dense_cur;
         HPD_CU(cudaMemsetAsync(da.n_dense, 0, sizeof(int), s));
         k_dense_list<<<blocks_for(m, 256), 256, 0, s>>>(cell_start, m, da);
-        k_dense_group<T><<<(unsigned)dense_max, 256, 0, s>>>(a, da);
+        k_dense_init<T><<<blocks_for(dense_max * da.groups, 256), 256, 0, s>>>(a, da);
+        k_dense_assign<T><<<blocks_for(n, 256), 256, 0, s>>>(a, da);
+        k_dense_offsets<T><<<blocks_for(dense_max, 4), 128, 0, s>>>(a, da);
+        k_dense_scatter<T><<<blocks_for(n, 256), 256, 0, s>>>(a, da);
+        k_mark_near_big<T><<<blocks_for(dense_max, 4), 128, 0, s>>>(a, da);
         a.dense_id = dense_id;
         a.dense_grp = dense_grp;
         a.dense_gidx = dense_gidx;
         a.dense_groups = da.groups;
-        info.launches += 2;
+        a.dense_sec = dense_sec;
+        a.dense_box = dense_box;
+        a.dense_coords = dense_coords;
+        a.dense_rep = dense_rep;
+        info.launches += 6;
     }
 
     // ---- core test (hpdbscan.h:72-78)
@@ -341,7 +392,11 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     } else if (rq.min_points > (uint64_t)n) {
         HPD_CU(cudaMemsetAsync(core, 0, n, s));
     } else {
-        HPD_QUERY_DISPATCH(k_core, T, mode, d, qgrid, 128, qsmem, s, a);
+        if (dense_k > 0) {
+            HPD_QUERY_DISPATCH_B(k_core, true, T, mode, d, qgrid, 128, qsmem, s, a);
+            info.launches += 1;
+        }
+        HPD_QUERY_DISPATCH_B(k_core, false, T, mode, d, qgrid, 128, qsmem, s, a);
         info.launches += 1;
     }
     if (timed) HPD_CU(cudaEventRecord(tm->ev[2], s));
@@ -349,13 +404,13 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     // ---- core-core connectivity
     k_iota<<<blocks_for(n, 256), 256, 0, s>>>(parent, n);
     if (dense_k > 0) {
-        k_dense_star<T><<<(unsigned)dense_max, 256, 0, s>>>(a, da);
+        k_dense_rep<T><<<blocks_for(n, 256), 256, 0, s>>>(a, da);
+        k_dense_link<T><<<blocks_for(n, 256), 256, 0, s>>>(a, da);
         HPD_QUERY_DISPATCH(k_dense_pairs, T, mode, d, blocks_for(dense_max, 4), 128, 0, s, a, da);
-        info.launches += 2;
+        info.launches += 3;
     }
     HPD_QUERY_DISPATCH(k_union_intra, T, mode, d, qgrid, 128, qsmem, s, a);
     k_fill_int<<<blocks_for(m, 256), 256, 0, s>>>(cell_rep, m, kNoCore);
-    HPD_CU(cudaMemsetAsync(cell_flags, kCellUniform, m, s));
     k_cell_rep<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep);
     k_cell_uniform<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep, cell_flags);
     HPD_QUERY_DISPATCH(k_union_cross, T, mode, d, qgrid, 128, qsmem, s, a);
@@ -365,7 +420,11 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
 
     // ---- borders
     HPD_CU(cudaMemsetAsync(flags_dev, 0, 6 * sizeof(int), s));
-    HPD_QUERY_DISPATCH(k_border, T, mode, d, qgrid, 128, qsmem, s, a);
+    if (dense_k > 0) {
+        HPD_QUERY_DISPATCH_B(k_border, true, T, mode, d, qgrid, 128, qsmem, s, a);
+        info.launches += 1;
+    }
+    HPD_QUERY_DISPATCH_B(k_border, false, T, mode, d, qgrid, 128, qsmem, s, a);
     info.launches += 1;
     int h_counts[7];  // [0] ambiguous borders, [6] cores
     HPD_CU(cudaMemcpyAsync(h_counts, flags_dev, sizeof h_counts, cudaMemcpyDeviceToHost, s));
@@ -473,8 +532,10 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 if (trace) {
                     unsigned long long tc[2];
                     int wn = 0;
-                    cudaMemcpy(tc, tcount, sizeof tc, cudaMemcpyDeviceToHost);
-                    cudaMemcpy(&wn, a.n_wlist, sizeof(int), cudaMemcpyDeviceToHost);
+                    // the engine's stream does not synchronise with the legacy default stream
+                    HPD_CU(cudaMemcpyAsync(tc, tcount, sizeof tc, cudaMemcpyDeviceToHost, s));
+                    HPD_CU(cudaMemcpyAsync(&wn, a.n_wlist, sizeof(int), cudaMemcpyDeviceToHost, s));
+                    HPD_CU(cudaStreamSynchronize(s));
                     fprintf(stderr, "[hpd tie] pass %d items %d active lanes %llu tiles %llu\n", pass,
                             pass == 1 ? n_items : wn, tc[0], tc[1]);
                 }

@@ -11,6 +11,7 @@
 #pragma once
 
 #include <climits>
+#include <type_traits>
 
 #include "hpd_common.cuh"
 #include "hpd_index.cuh"
@@ -51,6 +52,36 @@ __device__ __forceinline__ int find_cell(const CellTable& ct, unsigned long long
         if (ct.key[mid] < key) lo = mid + 1; else hi = mid;
     }
     return (lo < ct.m && ct.key[lo] == key) ? lo : -1;
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_xor_val(T v, int mask) {
+    if constexpr (sizeof(T) < 4) return (T)__shfl_xor_sync(0xffffffffu, (int)v, mask);
+    else return __shfl_xor_sync(0xffffffffu, v, mask);
+}
+
+// Warp-aggregated atomics: the lanes of a warp that target the same address combine
+// their values first, so that cells of millions of points cost one atomic per warp
+// rather than one per point.  Every lane of the warp must call; lanes with ok false
+// take no part in the update.
+__device__ __forceinline__ void agg_atomic_min(int* base, int idx, int v, bool ok) {
+    const unsigned peers = __match_any_sync(0xffffffffu, ok ? idx : -1);
+    if (!ok) return;
+    const int m = __reduce_min_sync(peers, v);
+    if ((int)lane_id() == __ffs(peers) - 1) atomicMin(base + idx, m);
+}
+__device__ __forceinline__ void agg_atomic_add(int* base, int idx, bool ok) {
+    const unsigned peers = __match_any_sync(0xffffffffu, ok ? idx : -1);
+    if (ok && (int)lane_id() == __ffs(peers) - 1) atomicAdd(base + idx, __popc(peers));
+}
+// slot of the lane among its peers: the leader reserves popc(peers) slots at base[idx]
+__device__ __forceinline__ int agg_reserve(int* base, int idx, bool ok) {
+    const unsigned peers = __match_any_sync(0xffffffffu, ok ? idx : -1);
+    const int leader = __ffs(peers) - 1;
+    int b = 0;
+    if (ok && (int)lane_id() == leader) b = atomicAdd(base + idx, __popc(peers));
+    b = __shfl_sync(0xffffffffu, b, leader);
+    return b + __popc(peers & ((1u << lane_id()) - 1u));
 }
 
 // Visits the non-empty cells of the 3^d block around cell r (sel: 0 all, 1 only
@@ -170,6 +201,10 @@ struct QueryArgs {
     const int* dense_grp; // [dense][groups + 1] sub-cell starts (see DenseArgs)
     const int* dense_gidx;  // per point of a dense cell: its sub-cell
     int dense_groups;
+    const int* dense_sec; // points of dense cells grouped by sub-cell (positions)
+    const T* dense_box;   // [dense][groups][2][d] bounding box of each sub-cell's points
+    const int* dense_rep; // [dense][groups] smallest core of each sub-cell (INT_MAX: none), after the core test
+    const T* dense_coords;  // [d][n] coordinates of dense cells' points in dense_sec order
     int* amb_out;         // undecided ambiguous borders after a decision round
     int* n_amb_out;
 };
@@ -179,6 +214,11 @@ struct QueryArgs {
 // coordinates (2 or 4 for d <= 4, so that one vector load fetches a candidate),
 // plus one aux word per candidate.
 __host__ __device__ __forceinline__ int tile_stride(int d) { return d <= 2 ? 2 : (d <= 4 ? 4 : d); }
+
+// cell summaries (cell_rep, cell_flags)
+constexpr int kNoCore = INT_MAX;
+constexpr uint8_t kCellUniform = 1;
+constexpr uint8_t kCellNearBig = 2;  // a cell of the 3^d block holds >= kPruneMinPoints points (dense path)
 
 template <typename T>
 struct Tile {
@@ -224,6 +264,80 @@ __device__ __forceinline__ bool scan_range(const QueryArgs<T>& a, const Tile<T>&
         const int cnt = min(32, ce - t0);
         for (int u = 0; u < cnt; ++u) pair(t0 + u, u, tile.aux[u]);
         __syncwarp();
+        if (done()) return true;
+    }
+    return false;
+}
+
+// Where a query lies relative to a sub-cell's bounding box: kBoxFar when every point
+// of the box is farther than eps, kBoxIn when every point is within eps, else
+// kBoxEdge.  The tests leave a 1e-4 relative margin on the squared distance; they run
+// in the element type (float or double), whose rounding (~1e-6 relative for float)
+// stays far inside that margin, so the verdict holds for the reference's own sum.
+constexpr int kBoxFar = 0, kBoxIn = 1, kBoxEdge = 2;
+template <typename T>
+using BoxReal = typename std::conditional<Elem<T>::kFloat, T, double>::type;
+template <typename T, int D>
+__device__ __forceinline__ int box_class(const T* q, const T* box, int d, BoxReal<T> eps2) {
+    using R = BoxReal<T>;
+    R lo2 = 0, hi2 = 0;
+#pragma unroll
+    for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+        if (D == 0 && k >= d) break;
+        const R lo = (R)box[k], hi = (R)box[d + k], x = (R)q[k];
+        const R dn = x < lo ? lo - x : (x > hi ? x - hi : R(0));
+        const R df = x - lo > hi - x ? x - lo : hi - x;
+        lo2 += dn * dn;
+        hi2 += df * df;
+    }
+    if (lo2 > eps2 * R(1.0001)) return kBoxFar;
+    return hi2 <= eps2 * R(0.9999) ? kBoxIn : kBoxEdge;
+}
+
+// Dense cells with at least this many points are visited sub-cell by sub-cell with the
+// box tests above; smaller ones are cheaper to stream whole.
+constexpr int kPruneMinPoints = 512;
+template <typename T>
+__device__ __forceinline__ bool pruned_cell(const QueryArgs<T>& a, int cr) {
+    return a.dense_id && a.dense_id[cr] >= 0 && a.ct.start[cr + 1] - a.ct.start[cr] >= kPruneMinPoints;
+}
+
+// Visits dense cell cr sub-cell by sub-cell: visit_group(g, cls) receives each lane's
+// box verdict for sub-cell g (kBoxFar for inactive lanes), may account for the whole
+// sub-cell, and returns whether the warp must stream its points through the tile
+// (warp-uniform).  pair(q, u, aux) gets the candidate's position q; returns true when
+// done() holds for the warp.
+template <typename T, int D, class Visit, class Aux, class Pair, class Done>
+__device__ __forceinline__ bool scan_dense(const QueryArgs<T>& a, const Tile<T>& tile, int cr, const T* q, bool active,
+                                           Visit&& visit_group, Aux&& aux_of, Pair&& pair, Done&& done) {
+    const int d = a.g.d;
+    const int S = tile_stride(d);
+    const unsigned lane = lane_id();
+    const int id = a.dense_id[cr];
+    const int s0 = a.ct.start[cr];
+    const int* grp = a.dense_grp + (size_t)id * (a.dense_groups + 1);
+    const T* box = a.dense_box + (size_t)id * a.dense_groups * 2 * d;
+    const int* idx = a.dense_sec + s0;
+    for (int g = 0; g < a.dense_groups; ++g) {
+        const int gs = grp[g], ge = grp[g + 1];
+        if (gs == ge) continue;
+        const int cls = active ? box_class<T, D>(q, box + (size_t)g * 2 * d, d, (BoxReal<T>)a.eps2) : kBoxFar;
+        if (visit_group(g, cls)) {
+            for (int t0 = gs; t0 < ge; t0 += 32) {
+                const int t = t0 + (int)lane;
+                int j = -1;
+                if (t < ge) {
+                    j = idx[t];
+                    for (int k = 0; k < d; ++k) tile.c[lane * S + k] = a.dense_coords[(size_t)k * a.n + s0 + t];
+                    tile.aux[lane] = aux_of(j);
+                }
+                __syncwarp();
+                const int cnt = min(32, ge - t0);
+                for (int u = 0; u < cnt; ++u) pair(__shfl_sync(0xffffffffu, j, u), u, tile.aux[u]);
+                __syncwarp();
+                if (done()) return true;
+            }
+        }
         if (done()) return true;
     }
     return false;
@@ -334,15 +448,17 @@ __device__ __forceinline__ T shfl_val(T v, int src) {
 constexpr int kSparseQueries = 8;  // items with at most this many points use candidate lanes
 constexpr int kMaxRanges = 32;     // neighbour ranges kept in shared memory (3^d <= 32: d <= 3)
 
-template <typename T, int M, int D>
+template <typename T, int M, int D, bool PRUNE>
 __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
     __shared__ int2 s_rng[4][kMaxRanges];
     const int w = threadIdx.x >> 5;
     const int item = blockIdx.x * 4 + w;
     if (item >= a.n_items) return;
-    const Tile<T> tile = warp_tile<T>(a.g.d);
     const int2 it = a.items[item];
     const int r = it.x;
+    // cells next to a big dense cell are handled by the PRUNE instantiation
+    if (((a.cell_flags[r] & kCellNearBig) != 0) != PRUNE) return;
+    const Tile<T> tile = warp_tile<T>(a.g.d);
     const int pend = min(it.y + 32, a.ct.start[r + 1]);
     const int p = it.y + (int)lane_id();
     const bool active = p < pend;
@@ -366,7 +482,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
     }
     int S = 1;
     for (int sd = 0; sd < a.g.d; ++sd) S *= 3;
-    if (pend - it.y <= kSparseQueries && S <= kMaxRanges) {
+    if (!PRUNE && pend - it.y <= kSparseQueries && S <= kMaxRanges) {
         // few queries: the whole warp tests consecutive candidates of one query at a
         // time (a ballot counts the hits), instead of leaving most lanes idle
         int nr = 0;
@@ -411,6 +527,24 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
     };
     auto done = [&]() { return __all_sync(0xffffffffu, !active || count >= limit); };
     visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
+        if constexpr (PRUNE) {
+            if (pruned_cell(a, cr)) {
+                // a sub-cell wholly within eps adds its population without a scan; only
+                // sub-cells crossing the eps sphere are streamed, for the lanes they cross
+                const int* grp = a.dense_grp + (size_t)a.dense_id[cr] * (a.dense_groups + 1);
+                int cur = kBoxFar;
+                auto visit_group = [&](int g, int cls) -> bool {
+                    cur = cls;
+                    if (cls == kBoxIn) count += grp[g + 1] - grp[g];
+                    return __any_sync(0xffffffffu, cls == kBoxEdge);
+                };
+                auto pair_edge = [&](int, int u, int) {
+                    if (cur == kBoxEdge && within<T, M, D>(a, q, tile, u)) ++count;
+                };
+                return !scan_dense<T, D>(a, tile, cr, q, active && count < limit, visit_group, aux_of, pair_edge,
+                                         done);
+            }
+        }
         return !scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
     });
     if (active) a.core[p] = count >= limit ? 1 : 0;
@@ -423,8 +557,6 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
 // and skips, without loading a single coordinate, a neighbour cell that holds no
 // core or whose cores are already in the query cell's component.  Within a tile,
 // candidates already in the query's component are skipped without a distance test.
-constexpr int kNoCore = INT_MAX;
-constexpr uint8_t kCellUniform = 1;
 
 template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_union_intra(QueryArgs<T> a) {
@@ -455,7 +587,8 @@ __global__ void __launch_bounds__(128) k_union_intra(QueryArgs<T> a) {
 
 static __global__ void k_cell_rep(const uint8_t* core, int* parent, const uint32_t* cellrank, int n, int* cell_rep) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && core[i]) atomicMin(cell_rep + cellrank[i], uf_find(parent, i));
+    const bool ok = i < n && core[i];
+    agg_atomic_min(cell_rep, ok ? (int)cellrank[i] : 0, ok ? uf_find(parent, i) : 0, ok);
 }
 
 static __global__ void k_cell_uniform(const uint8_t* core, int* parent, const uint32_t* cellrank, int n,
@@ -463,7 +596,8 @@ static __global__ void k_cell_uniform(const uint8_t* core, int* parent, const ui
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n && core[i]) {
         const uint32_t c = cellrank[i];
-        if (uf_find(parent, i) != cell_rep[c]) cell_flags[c] = 0;
+        // every writer clears the same bit of a byte whose other bits no longer change
+        if (uf_find(parent, i) != cell_rep[c]) cell_flags[c] &= (uint8_t)~kCellUniform;
     }
 }
 
@@ -489,6 +623,9 @@ struct DenseArgs {
     int* grp_rep;           // [dense][groups] smallest core of each sub-cell (INT_MAX: none)
     int* sec;               // points of dense cells grouped by sub-cell (same range as the cell)
     int* gidx;              // per point of a dense cell: its sub-cell
+    void* box;              // [dense][groups][2][d] element-type bounding box of each sub-cell
+    void* coords;           // [d][n] coordinates of dense cells' points in sec order
+    int* cur;               // [dense][groups] scatter cursors
 };
 
 static __global__ void k_dense_list(const int32_t* cell_start, int m, DenseArgs da) {
@@ -503,21 +640,66 @@ static __global__ void k_dense_list(const int32_t* cell_start, int m, DenseArgs 
     }
 }
 
-// block per dense cell: sub-cell of every point and a counting sort of the cell's
-// points by sub-cell into sec (runs before the core test, which uses the counts)
+// Order-preserving unsigned encoding of a floating value (larger value, larger code),
+// so that integer atomics can take minima and maxima of coordinates.
+template <typename T> struct OrdKey;
+template <> struct OrdKey<float> {
+    using U = unsigned;
+    __device__ static U enc(float v) {
+        const unsigned u = __float_as_uint(v);
+        return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    }
+    __device__ static float dec(U u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u); }
+};
+template <> struct OrdKey<double> {
+    using U = unsigned long long;
+    __device__ static U enc(double v) {
+        const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+        return (u >> 63) ? ~u : (u | (1ull << 63));
+    }
+    __device__ static double dec(U u) { return __longlong_as_double((long long)((u >> 63) ? (u & ~(1ull << 63)) : ~u)); }
+};
+
+constexpr int kDenseMaxGroups = 81;  // k^d for the sub-cell splits used (<= 81)
+
+// Sub-cell construction for all dense cells at once, parallel over points (a cell of
+// millions of points is spread over the whole GPU):
+//   k_dense_init     per (dense cell, sub-cell): count 0, no core, empty box
+//   k_dense_assign   per point of a dense cell: its sub-cell, the count, the box
+//   k_dense_offsets  per dense cell: counts -> start offsets, boxes decoded
+//   k_dense_scatter  per point: its slot in sec and its coordinates in sec order
 template <typename T>
-__global__ void __launch_bounds__(256) k_dense_group(QueryArgs<T> a, DenseArgs da) {
-    __shared__ int cnt[256];
-    __shared__ int cur[256];
-    const int id = blockIdx.x;
-    if (id >= *da.n_dense) return;
-    const int c = da.cells[id];
-    const int s0 = a.ct.start[c], s1 = a.ct.start[c + 1];
-    for (int g = threadIdx.x; g < da.groups; g += blockDim.x) cnt[g] = 0;
-    __syncthreads();
-    for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-        int g = 0, mul = 1;
-        for (int sd = 0; sd < a.g.d; ++sd) {
+__global__ void k_dense_init(QueryArgs<T> a, DenseArgs da) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)*da.n_dense * da.groups) return;
+    const int64_t id = t / da.groups, g = t - id * da.groups;
+    da.grp[id * (da.groups + 1) + g] = 0;
+    if (g == 0) da.grp[id * (da.groups + 1) + da.groups] = 0;
+    da.grp_rep[t] = INT_MAX;
+    if constexpr (Elem<T>::kFloat) {
+        using U = typename OrdKey<T>::U;
+        U* box = static_cast<U*>(da.box) + (size_t)t * 2 * a.g.d;
+        for (int k = 0; k < a.g.d; ++k) {
+            box[k] = ~U(0);
+            box[a.g.d + k] = U(0);
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dense_assign(QueryArgs<T> a, DenseArgs da) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = a.g.d;
+    bool ok = i < a.n;
+    int c = 0, id = -1, g = 0;
+    if (ok) {
+        c = (int)a.cellrank[i];
+        id = da.dense_id[c];
+        ok = id >= 0;
+    }
+    if (ok) {
+        int mul = 1;
+        for (int sd = 0; sd < d; ++sd) {
             const int j = a.g.swapped[sd];
             const double v = ((double)a.coords[(size_t)j * a.n + i] - da.mins_d[j]) * da.scale;
             long long sub = (long long)floor(v) - (long long)da.k * (long long)a.ct.ccoord[(size_t)sd * a.ct.pitch + c];
@@ -526,45 +708,121 @@ __global__ void __launch_bounds__(256) k_dense_group(QueryArgs<T> a, DenseArgs d
             mul *= da.k;
         }
         da.gidx[i] = g;
-        atomicAdd(&cnt[g], 1);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int run = 0;
-        for (int g = 0; g < da.groups; ++g) {
-            da.grp[(size_t)id * (da.groups + 1) + g] = run;
-            cur[g] = run;
-            run += cnt[g];
+    agg_atomic_add(da.grp, ok ? id * (da.groups + 1) + g : 0, ok);
+    if constexpr (Elem<T>::kFloat) {
+        using U = typename OrdKey<T>::U;
+        U* box = static_cast<U*>(da.box) + ((size_t)(ok ? id : 0) * da.groups + g) * 2 * d;
+        const unsigned peers = __match_any_sync(0xffffffffu, ok ? id * da.groups + g : -1);
+        const bool leader = (int)lane_id() == __ffs(peers) - 1;
+        for (int k = 0; k < d; ++k) {
+            const U kv = ok ? OrdKey<T>::enc(a.coords[(size_t)k * a.n + i]) : U(0);
+            if constexpr (sizeof(U) == 4) {
+                if (ok) {
+                    const U lo = __reduce_min_sync(peers, kv), hi = __reduce_max_sync(peers, kv);
+                    if (leader) {
+                        atomicMin(box + k, lo);
+                        atomicMax(box + d + k, hi);
+                    }
+                }
+            } else if (ok) {
+                atomicMin(box + k, kv);
+                atomicMax(box + d + k, kv);
+            }
         }
-        da.grp[(size_t)id * (da.groups + 1) + da.groups] = run;
-    }
-    __syncthreads();
-    for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-        const int g = da.gidx[i];
-        da.sec[s0 + atomicAdd(&cur[g], 1)] = i;
     }
 }
 
-// block per dense cell: the smallest core of every sub-cell becomes the root of a star
-// over the sub-cell's cores (they are pairwise within eps); runs before any union
 template <typename T>
-__global__ void __launch_bounds__(256) k_dense_star(QueryArgs<T> a, DenseArgs da) {
-    __shared__ int rep[256];
-    const int id = blockIdx.x;
+__global__ void __launch_bounds__(128) k_dense_offsets(QueryArgs<T> a, DenseArgs da) {
+    const int id = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (id >= *da.n_dense) return;
+    const int lane = (int)lane_id();
+    int* grp = da.grp + (size_t)id * (da.groups + 1);
+    int run = 0;
+    for (int g0 = 0; g0 < da.groups; g0 += 32) {
+        const int g = g0 + lane;
+        const int v = g < da.groups ? grp[g] : 0;
+        int inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (g < da.groups) {
+            grp[g] = run + inc - v;
+            da.cur[(size_t)id * da.groups + g] = run + inc - v;
+        }
+        run += __shfl_sync(0xffffffffu, inc, 31);
+    }
+    if (lane == 0) grp[da.groups] = run;
+    if constexpr (Elem<T>::kFloat) {
+        using U = typename OrdKey<T>::U;
+        const size_t nb = (size_t)da.groups * 2 * a.g.d;
+        U* key = static_cast<U*>(da.box) + (size_t)id * nb;
+        T* val = static_cast<T*>(da.box) + (size_t)id * nb;
+        for (size_t t = lane; t < nb; t += 32) val[t] = OrdKey<T>::dec(key[t]);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dense_scatter(QueryArgs<T> a, DenseArgs da) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool ok = i < a.n;
+    int c = 0, id = -1;
+    if (ok) {
+        c = (int)a.cellrank[i];
+        id = da.dense_id[c];
+        ok = id >= 0;
+    }
+    const int g = ok ? da.gidx[i] : 0;
+    const int slot = agg_reserve(da.cur, ok ? id * da.groups + g : 0, ok);
+    if (ok) {
+        const int s0 = a.ct.start[c];
+        da.sec[s0 + slot] = (int)i;
+        T* dc = static_cast<T*>(da.coords);
+        for (int k = 0; k < a.g.d; ++k) dc[(size_t)k * a.n + s0 + slot] = a.coords[(size_t)k * a.n + i];
+    }
+}
+
+// Stars over the sub-cell cliques (after the core test, before any other union): the
+// smallest core of every sub-cell (k_dense_rep) becomes the parent of the others
+// (k_dense_link).  Parallel over points.
+template <typename T>
+__global__ void __launch_bounds__(256) k_dense_rep(QueryArgs<T> a, DenseArgs da) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool ok = i < a.n && a.core[i];
+    int id = -1;
+    if (ok) {
+        id = da.dense_id[a.cellrank[i]];
+        ok = id >= 0;
+    }
+    agg_atomic_min(da.grp_rep, ok ? id * da.groups + da.gidx[i] : 0, (int)i, ok);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dense_link(QueryArgs<T> a, DenseArgs da) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !a.core[i]) return;
+    const int id = da.dense_id[a.cellrank[i]];
+    if (id < 0) return;
+    const int r = da.grp_rep[(size_t)id * da.groups + da.gidx[i]];
+    if (r != (int)i) a.parent[i] = r;
+}
+
+// warp per dense cell: a cell with >= kPruneMinPoints points flags every cell of its
+// 3^d block (itself included) with kCellNearBig.  Every writer sets the same bit of a
+// byte whose other bit no longer changes, so the unsynchronised updates agree.
+template <typename T>
+__global__ void __launch_bounds__(128) k_mark_near_big(QueryArgs<T> a, DenseArgs da) {
+    const int id = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (id >= *da.n_dense) return;
     const int c = da.cells[id];
-    const int s0 = a.ct.start[c], s1 = a.ct.start[c + 1];
-    for (int g = threadIdx.x; g < da.groups; g += blockDim.x) rep[g] = INT_MAX;
-    __syncthreads();
-    for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x)
-        if (a.core[i]) atomicMin(&rep[da.gidx[i]], i);
-    __syncthreads();
-    for (int g = threadIdx.x; g < da.groups; g += blockDim.x) da.grp_rep[(size_t)id * da.groups + g] = rep[g];
-    for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-        if (!a.core[i]) continue;
-        const int r = rep[da.gidx[i]];
-        if (r != i) a.parent[i] = r;
-    }
+    if (a.ct.start[c + 1] - a.ct.start[c] < kPruneMinPoints) return;
+    visit_stencil(a.g, a.ct, c, 0, [&](int cr, bool) {
+        if (lane_id() == 0) a.cell_flags[cr] |= kCellNearBig;
+        return true;
+    });
 }
 
 template <typename T, int M, int D>
@@ -586,38 +844,90 @@ __device__ __forceinline__ bool within_pts(const QueryArgs<T>& a, int i, int j) 
 
 __device__ __forceinline__ bool same_component(int* parent, int x, int y);
 
-// warp per dense cell: connect its sub-cells pairwise (first core-core eps pair found)
+// squared distance between two sub-cell boxes exceeds eps^2 (with the box-test margin)
+template <typename T>
+__device__ __forceinline__ bool boxes_apart(const T* b1, const T* b2, int d, BoxReal<T> eps2) {
+    using R = BoxReal<T>;
+    R s2 = 0;
+    for (int k = 0; k < d; ++k) {
+        R gap = (R)b2[k] - (R)b1[d + k];
+        const R g2 = (R)b1[k] - (R)b2[d + k];
+        gap = gap > g2 ? gap : g2;
+        if (gap > R(0)) s2 += gap * gap;
+    }
+    return s2 > eps2 * R(1.0001);
+}
+
+// warp per dense cell: connect its sub-cells pairwise.  Sub-cell pairs whose boxes are
+// farther apart than eps, or already in one component, are skipped; otherwise the
+// lanes take 32 cores of the first sub-cell at a time (those within reach of the
+// second sub-cell's box) and stream the second sub-cell's cores past them until one
+// core-core eps pair is found, which is united.
 template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_dense_pairs(QueryArgs<T> a, DenseArgs da) {
     const int id = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (id >= *da.n_dense) return;
     const unsigned lane = lane_id();
+    const int d = a.g.d;
     const int c = da.cells[id];
     const int s0 = a.ct.start[c];
     const int* grp = da.grp + (size_t)id * (da.groups + 1);
     const int* rep = da.grp_rep + (size_t)id * da.groups;
+    const T* box = a.dense_box + (size_t)id * da.groups * 2 * d;
+    const BoxReal<T> eps2 = (BoxReal<T>)a.eps2;
     for (int g1 = 0; g1 < da.groups; ++g1) {
         if (rep[g1] == INT_MAX) continue;
         for (int g2 = g1 + 1; g2 < da.groups; ++g2) {
             if (rep[g2] == INT_MAX) continue;
+            if (boxes_apart(box + (size_t)g1 * 2 * d, box + (size_t)g2 * 2 * d, d, eps2)) continue;
             if (same_component(a.parent, rep[g1], rep[g2])) continue;
             bool joined = false;
-            for (int x = grp[g1]; x < grp[g1 + 1] && !joined; ++x) {
-                const int pa = da.sec[s0 + x];
-                if (!a.core[pa]) continue;
+            for (int x0 = grp[g1]; x0 < grp[g1 + 1] && !joined; x0 += 32) {
+                const int x = x0 + (int)lane;
+                int pa = -1;
+                T qa[D > 0 ? D : kMaxDims];
+                if (x < grp[g1 + 1]) {
+                    pa = da.sec[s0 + x];
+#pragma unroll
+                    for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                        if (D == 0 && k >= d) break;
+                        qa[k] = a.dense_coords[(size_t)k * a.n + s0 + x];
+                    }
+                    if (!a.core[pa] || box_class<T, D>(qa, box + (size_t)g2 * 2 * d, d, eps2) == kBoxFar) pa = -1;
+                }
+                if (!__any_sync(0xffffffffu, pa >= 0)) continue;
                 for (int y0 = grp[g2]; y0 < grp[g2 + 1] && !joined; y0 += 32) {
                     const int y = y0 + (int)lane;
                     int pb = -1;
+                    T cb[D > 0 ? D : kMaxDims];
                     if (y < grp[g2 + 1]) {
                         pb = da.sec[s0 + y];
-                        if (!a.core[pb] || !within_pts<T, M, D>(a, pa, pb)) pb = -1;
+                        if (!a.core[pb]) pb = -1;
+#pragma unroll
+                        for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                            if (D == 0 && k >= d) break;
+                            cb[k] = a.dense_coords[(size_t)k * a.n + s0 + y];
+                        }
                     }
-                    const unsigned hit = __ballot_sync(0xffffffffu, pb >= 0);
-                    if (hit) {
-                        const int other = __shfl_sync(0xffffffffu, pb, __ffs(hit) - 1);
-                        if (lane == 0) uf_union(a.parent, pa, other);
-                        __syncwarp();
-                        joined = true;
+                    unsigned cand = __ballot_sync(0xffffffffu, pb >= 0);
+                    while (cand && !joined) {
+                        const int u = __ffs(cand) - 1;
+                        cand &= cand - 1;
+                        T cu[D > 0 ? D : kMaxDims];
+#pragma unroll
+                        for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                            if (D == 0 && k >= d) break;
+                            cu[k] = shfl_val(cb[k], u);
+                        }
+                        const unsigned hit = __ballot_sync(0xffffffffu, pa >= 0 && within_vals<T, M, D>(a, qa, cu));
+                        if (hit) {
+                            const int src = __ffs(hit) - 1;
+                            const int xa = __shfl_sync(0xffffffffu, pa, src);
+                            const int yb = __shfl_sync(0xffffffffu, pb, u);
+                            if (lane == 0) uf_union(a.parent, xa, yb);
+                            __syncwarp();
+                            joined = true;
+                        }
                     }
                 }
             }
@@ -681,12 +991,14 @@ static __global__ void k_compress(int* parent, const uint8_t* core, int n, int* 
 // A non-core point with core neighbours of a single component joins it; with
 // several it is recorded as ambiguous for the tie-break.  Cells without cores,
 // and single-component cells of the component already found, are skipped.
-template <typename T, int M, int D>
+template <typename T, int M, int D, bool PRUNE>
 __global__ void __launch_bounds__(128) k_border(QueryArgs<T> a) {
     const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (item >= a.n_items) return;
     const int2 it = a.items[item];
     const int r = it.x;
+    // cells next to a big dense cell are handled by the PRUNE instantiation
+    if (((a.cell_flags[r] & kCellNearBig) != 0) != PRUNE) return;
     const int pend = min(it.y + 32, a.ct.start[r + 1]);
     const int p = it.y + (int)lane_id();
     const bool active = p < pend && !a.core[p];
@@ -697,20 +1009,44 @@ __global__ void __launch_bounds__(128) k_border(QueryArgs<T> a) {
     int r1 = -1;
     bool multi = false;
     auto aux_of = [&](int j) { return a.core[j] ? a.parent[j] : -1; };
+    auto hit = [&](int rep) {  // a core of component rep lies within eps
+        if (r1 < 0) r1 = rep;
+        else if (rep != r1) { multi = true; r1 = min(r1, rep); }
+    };
     auto pair = [&](int, int u, int rep) {
         if (!active || multi || rep < 0 || rep == r1) return;
-        if (within<T, M, D>(a, q, tile, u)) {
-            if (r1 < 0) r1 = rep;
-            else { multi = true; r1 = min(r1, rep); }
-        }
+        if (within<T, M, D>(a, q, tile, u)) hit(rep);
     };
     auto done = [&]() { return __all_sync(0xffffffffu, !active || multi); };
     visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
         const int rep_c = a.cell_rep[cr];
         if (rep_c == kNoCore) return true;
+        const bool dense = PRUNE && pruned_cell(a, cr);
+        // sub-cells are cliques, so the cores of one sub-cell share a component: a
+        // sub-cell wholly within eps that holds a core is a hit without a scan
+        const int* grep = dense ? a.dense_rep + (size_t)a.dense_id[cr] * a.dense_groups : nullptr;
+        auto visit_group = [&](int g, int cls) -> bool {
+            const int rc = grep[g];
+            if (rc == INT_MAX) return false;  // no core in the sub-cell
+            if (cls == kBoxIn && !multi) hit(a.parent[rc]);
+            return __any_sync(0xffffffffu, cls == kBoxEdge && !multi);
+        };
         if (a.cell_flags[cr] & kCellUniform) {
+            // every core of the cell is in component root_c: once each lane holds it
+            // (or two clusters), the rest of the cell changes nothing
             const int root_c = a.parent[rep_c];
-            if (__all_sync(0xffffffffu, !active || multi || r1 == root_c)) return true;
+            auto cell_done = [&]() { return __all_sync(0xffffffffu, !active || multi || r1 == root_c); };
+            if (cell_done()) return true;
+            if constexpr (PRUNE) {
+                if (dense) scan_dense<T, D>(a, tile, cr, q, active && !multi, visit_group, aux_of, pair, cell_done);
+                else scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, cell_done);
+            } else {
+                scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, cell_done);
+            }
+            return !done();
+        }
+        if constexpr (PRUNE) {
+            if (dense) return !scan_dense<T, D>(a, tile, cr, q, active && !multi, visit_group, aux_of, pair, done);
         }
         return !scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
     }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore; });
@@ -974,14 +1310,18 @@ __global__ void k_tie_jump(QueryArgs<T> a) {
 template <typename T>
 __global__ void k_tie_cell_min(QueryArgs<T> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n || !a.core[i]) return;
-    const int c = (int)a.cellrank[i];
-    if (!in_range(a.guard, c, a.ct.m, kGuardCellRank)) return;
-    atomicMin(a.cell_min_l + c, a.lm1[i]);
-    const int s0 = a.ct.start[c];
-    const int ti = (int)a.ipos[s0] + ((i - s0) >> 5);
-    if (!in_range(a.guard, ti, a.n_items, kGuardItemIndex)) return;
-    atomicMin(a.item_min_l + ti, a.lm1[i]);
+    bool ok = i < a.n && a.core[i];
+    const int c = ok ? (int)a.cellrank[i] : 0;
+    if (ok && !in_range(a.guard, c, a.ct.m, kGuardCellRank)) ok = false;
+    const int v = ok ? a.lm1[i] : 0;
+    agg_atomic_min(a.cell_min_l, c, v, ok);
+    int ti = 0;
+    if (ok) {
+        const int s0 = a.ct.start[c];
+        ti = (int)a.ipos[s0] + ((i - s0) >> 5);
+        if (!in_range(a.guard, ti, a.n_items, kGuardItemIndex)) ok = false;
+    }
+    agg_atomic_min(a.item_min_l, ti, v, ok);
 }
 
 // Next pass's work: the items of every cell whose lower stencil or own cell was

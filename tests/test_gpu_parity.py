@@ -144,3 +144,21 @@ def test_gpu_stats_counts(gpu, oracle):
     assert st["n_core"] == int((labels < 0).sum())
     _, _, cells = oracle.cluster(pts, eps, mp, with_order=True)
     assert st["n_cells"] == len(np.unique(cells))
+
+
+@pytest.mark.parametrize("d,dtype,k", [(2, np.float32, 0), (3, np.float32, 1), (4, np.float32, 2),
+                                       (2, np.float64, 3), (3, np.float32, 4)])
+def test_gpu_big_cells(gpu, oracle, d, dtype, k):
+    """Cells of thousands of points (compact blobs, sigma ~ eps / 10) ringed by points at
+    every distance: the box-certified counts, hits and pruning of big cells give the
+    oracle's labels."""
+    rng = np.random.default_rng(40 + k)
+    eps = 0.01
+    centres = rng.random((6, d)) * 0.5 + 0.25
+    blobs = [c + rng.normal(0, eps * rng.uniform(0.05, 0.3), (int(rng.integers(2000, 9000)), d)) for c in centres]
+    ring = np.concatenate([c + rng.uniform(-3 * eps, 3 * eps, (1500, d)) for c in centres])
+    pts = np.concatenate(blobs + [ring, rng.random((3000, d))]).astype(dtype)
+    pts = pts[rng.permutation(len(pts))]
+    for mp in (4, 40, 400):
+        want = oracle.cluster(pts, eps, mp, threads=1)
+        assert np.array_equal(engine(eps, mp).cluster_array(pts), want), mp
