@@ -312,6 +312,8 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         dense_k = fine_k;
         dense_groups = groups_cap;
     }
+    // cells of >= kPruneMinPoints points get sub-cell boxes and the pruned query paths
+    const bool prune = dense_k > 0 && h_tot[2] >= (uint32_t)kPruneMinPoints;
     info.n_cells = m;
     if (timed) HPD_CU(cudaEventRecord(tm->ev[1], s));
 
@@ -368,13 +370,14 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         da.box = dense_box;
         da.coords = dense_coords;
         da.cur = dense_cur;
+        da.boxes = prune ? 1 : 0;
         HPD_CU(cudaMemsetAsync(da.n_dense, 0, sizeof(int), s));
         k_dense_list<<<blocks_for(m, 256), 256, 0, s>>>(cell_start, m, da);
         k_dense_init<T><<<blocks_for(dense_max * da.groups, 256), 256, 0, s>>>(a, da);
         k_dense_assign<T><<<blocks_for(n, 256), 256, 0, s>>>(a, da);
         k_dense_offsets<T><<<blocks_for(dense_max, 4), 128, 0, s>>>(a, da);
         k_dense_scatter<T><<<blocks_for(n, 256), 256, 0, s>>>(a, da);
-        k_mark_near_big<T><<<blocks_for(dense_max, 4), 128, 0, s>>>(a, da);
+        if (prune) k_mark_near_big<T><<<blocks_for(dense_max, 4), 128, 0, s>>>(a, da);
         a.dense_id = dense_id;
         a.dense_grp = dense_grp;
         a.dense_gidx = dense_gidx;
@@ -383,7 +386,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         a.dense_box = dense_box;
         a.dense_coords = dense_coords;
         a.dense_rep = dense_rep;
-        info.launches += 6;
+        info.launches += prune ? 6 : 5;
     }
 
     // ---- core test (hpdbscan.h:72-78)
@@ -392,7 +395,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     } else if (rq.min_points > (uint64_t)n) {
         HPD_CU(cudaMemsetAsync(core, 0, n, s));
     } else {
-        if (dense_k > 0) {
+        if (prune) {
             HPD_QUERY_DISPATCH_B(k_core, true, T, mode, d, qgrid, 128, qsmem, s, a);
             info.launches += 1;
         }
@@ -420,7 +423,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
 
     // ---- borders
     HPD_CU(cudaMemsetAsync(flags_dev, 0, 6 * sizeof(int), s));
-    if (dense_k > 0) {
+    if (prune) {
         HPD_QUERY_DISPATCH_B(k_border, true, T, mode, d, qgrid, 128, qsmem, s, a);
         info.launches += 1;
     }

@@ -296,7 +296,7 @@ __device__ __forceinline__ int box_class(const T* q, const T* box, int d, BoxRea
 
 // Dense cells with at least this many points are visited sub-cell by sub-cell with the
 // box tests above; smaller ones are cheaper to stream whole.
-constexpr int kPruneMinPoints = 512;
+constexpr int kPruneMinPoints = 8192;
 template <typename T>
 __device__ __forceinline__ bool pruned_cell(const QueryArgs<T>& a, int cr) {
     return a.dense_id && a.dense_id[cr] >= 0 && a.ct.start[cr + 1] - a.ct.start[cr] >= kPruneMinPoints;
@@ -626,6 +626,7 @@ struct DenseArgs {
     void* box;              // [dense][groups][2][d] element-type bounding box of each sub-cell
     void* coords;           // [d][n] coordinates of dense cells' points in sec order
     int* cur;               // [dense][groups] scatter cursors
+    int boxes;              // build boxes and the coordinate copy (a cell holds >= kPruneMinPoints)
 };
 
 static __global__ void k_dense_list(const int32_t* cell_start, int m, DenseArgs da) {
@@ -677,6 +678,7 @@ __global__ void k_dense_init(QueryArgs<T> a, DenseArgs da) {
     if (g == 0) da.grp[id * (da.groups + 1) + da.groups] = 0;
     da.grp_rep[t] = INT_MAX;
     if constexpr (Elem<T>::kFloat) {
+        if (!da.boxes) return;
         using U = typename OrdKey<T>::U;
         U* box = static_cast<U*>(da.box) + (size_t)t * 2 * a.g.d;
         for (int k = 0; k < a.g.d; ++k) {
@@ -710,6 +712,7 @@ __global__ void __launch_bounds__(256) k_dense_assign(QueryArgs<T> a, DenseArgs 
         da.gidx[i] = g;
     }
     agg_atomic_add(da.grp, ok ? id * (da.groups + 1) + g : 0, ok);
+    if (!da.boxes) return;
     if constexpr (Elem<T>::kFloat) {
         using U = typename OrdKey<T>::U;
         U* box = static_cast<U*>(da.box) + ((size_t)(ok ? id : 0) * da.groups + g) * 2 * d;
@@ -756,6 +759,7 @@ __global__ void __launch_bounds__(128) k_dense_offsets(QueryArgs<T> a, DenseArgs
         run += __shfl_sync(0xffffffffu, inc, 31);
     }
     if (lane == 0) grp[da.groups] = run;
+    if (!da.boxes) return;
     if constexpr (Elem<T>::kFloat) {
         using U = typename OrdKey<T>::U;
         const size_t nb = (size_t)da.groups * 2 * a.g.d;
@@ -780,8 +784,10 @@ __global__ void __launch_bounds__(256) k_dense_scatter(QueryArgs<T> a, DenseArgs
     if (ok) {
         const int s0 = a.ct.start[c];
         da.sec[s0 + slot] = (int)i;
-        T* dc = static_cast<T*>(da.coords);
-        for (int k = 0; k < a.g.d; ++k) dc[(size_t)k * a.n + s0 + slot] = a.coords[(size_t)k * a.n + i];
+        if (da.boxes) {
+            T* dc = static_cast<T*>(da.coords);
+            for (int k = 0; k < a.g.d; ++k) dc[(size_t)k * a.n + s0 + slot] = a.coords[(size_t)k * a.n + i];
+        }
     }
 }
 
@@ -879,7 +885,7 @@ __global__ void __launch_bounds__(128) k_dense_pairs(QueryArgs<T> a, DenseArgs d
         if (rep[g1] == INT_MAX) continue;
         for (int g2 = g1 + 1; g2 < da.groups; ++g2) {
             if (rep[g2] == INT_MAX) continue;
-            if (boxes_apart(box + (size_t)g1 * 2 * d, box + (size_t)g2 * 2 * d, d, eps2)) continue;
+            if (da.boxes && boxes_apart(box + (size_t)g1 * 2 * d, box + (size_t)g2 * 2 * d, d, eps2)) continue;
             if (same_component(a.parent, rep[g1], rep[g2])) continue;
             bool joined = false;
             for (int x0 = grp[g1]; x0 < grp[g1 + 1] && !joined; x0 += 32) {
@@ -891,9 +897,10 @@ __global__ void __launch_bounds__(128) k_dense_pairs(QueryArgs<T> a, DenseArgs d
 #pragma unroll
                     for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
                         if (D == 0 && k >= d) break;
-                        qa[k] = a.dense_coords[(size_t)k * a.n + s0 + x];
+                        qa[k] = a.coords[(size_t)k * a.n + pa];
                     }
-                    if (!a.core[pa] || box_class<T, D>(qa, box + (size_t)g2 * 2 * d, d, eps2) == kBoxFar) pa = -1;
+                    if (!a.core[pa] || (da.boxes && box_class<T, D>(qa, box + (size_t)g2 * 2 * d, d, eps2) == kBoxFar))
+                        pa = -1;
                 }
                 if (!__any_sync(0xffffffffu, pa >= 0)) continue;
                 for (int y0 = grp[g2]; y0 < grp[g2 + 1] && !joined; y0 += 32) {
@@ -901,12 +908,12 @@ __global__ void __launch_bounds__(128) k_dense_pairs(QueryArgs<T> a, DenseArgs d
                     int pb = -1;
                     T cb[D > 0 ? D : kMaxDims];
                     if (y < grp[g2 + 1]) {
-                        pb = da.sec[s0 + y];
-                        if (!a.core[pb]) pb = -1;
+                        const int j = da.sec[s0 + y];
+                        pb = a.core[j] ? j : -1;
 #pragma unroll
                         for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
                             if (D == 0 && k >= d) break;
-                            cb[k] = a.dense_coords[(size_t)k * a.n + s0 + y];
+                            cb[k] = a.coords[(size_t)k * a.n + j];
                         }
                     }
                     unsigned cand = __ballot_sync(0xffffffffu, pb >= 0);

@@ -156,6 +156,7 @@ def test_gpu_big_cells(gpu, oracle, d, dtype, k):
     eps = 0.01
     centres = rng.random((6, d)) * 0.5 + 0.25
     blobs = [c + rng.normal(0, eps * rng.uniform(0.05, 0.3), (int(rng.integers(2000, 9000)), d)) for c in centres]
+    blobs[0] = centres[0] + rng.normal(0, eps * 0.05, (12000, d))  # one cell above the pruning size
     ring = np.concatenate([c + rng.uniform(-3 * eps, 3 * eps, (1500, d)) for c in centres])
     pts = np.concatenate(blobs + [ring, rng.random((3000, d))]).astype(dtype)
     pts = pts[rng.permutation(len(pts))]
