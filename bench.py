@@ -14,6 +14,9 @@ out) on the same workload.  With --gpus N > 1 (torchrun) every rank clusters its
 replica of the workload (no data-path collective; the path does not shard) and the
 job value is N x points / the slowest rank's time.
 
+`skewed` times the 50M-point skewed 2-D density workload (cells of up to 2.2M points) the
+same way as `value`.
+
 --impl reference times the CPU implementation of the same path on the host cores:
 the upstream build when it exists on this host, else the C restatement run with the
 upstream's parallel structure (OpenMP, all host threads), on a spatial crop of the
@@ -240,6 +243,37 @@ def measure_served(duration_s, workers, rate=200.0):
             "plain": {k: plain[k] for k in ("jobs_per_s", "p50_ms", "p99_ms", "makespan_s")}}
 
 
+def measure_skewed(n_points, steps=3):
+    """Skewed 2-D density workload (1,000 anisotropic Gaussians, Zipf weights, 2 % noise,
+    eps 1e-3, minPoints 32; cells of up to 2.2M points at 50M): device-resident input,
+    CUDA events on the engine's stream, L2 flushed between steps."""
+    import torch
+    from hpdbscan_gb300 import HPDBSCAN, workloads
+    w = workloads.skewed_2d(seed=0, n=n_points)
+    n, d = w.points.shape
+    h = HPDBSCAN(w.eps, w.min_points)
+    stream = torch.cuda.current_stream()
+    x = torch.from_numpy(w.points).cuda()
+    labels = torch.empty(n, dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(2):
+        h.cluster_device(x.data_ptr(), n, d, np.float32, labels.data_ptr(), stream.cuda_stream)
+    ms = []
+    for _ in range(steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.cluster_device(x.data_ptr(), n, d, np.float32, labels.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    st = h.stats()
+    t = sum(ms) / len(ms)
+    return {"workload": f"skewed_2d: {n:,} x 2 float32, eps 1e-3, minPoints 32, seed 0", "ms_per_step": t,
+            "mpoints_per_s": n / t / 1e3, "steps": steps,
+            "phases_ms": {k: round(st[k + "_ms"], 3) for k in ("index", "core", "union", "border", "tie", "finalize")}}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -368,6 +402,8 @@ def run_engine(args):
     batched = measure_batched(args.batch_instances, 8) if args.batch_instances > 0 else None
     progress("served trace")
     served = measure_served(args.serve_seconds, 8) if args.serve_seconds > 0 else None
+    progress("skewed density")
+    skewed = measure_skewed(args.skewed_points) if args.skewed_points > 0 else None
     progress("done")
     line = {
         "metric": METRIC, "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": args.steps,
@@ -389,6 +425,7 @@ def run_engine(args):
                                    f"({CROP:.0%}), median of 2 runs"},
         "batched": batched,
         "served": served,
+        "skewed": skewed,
         "gpu_launches": launches,
         "clocks": clock.summary(local),
         "wall_s": wall,
@@ -406,6 +443,7 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--batch-instances", type=int, default=256, help="batch workload instances (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="length of the serving trace (0: skip)")
+    ap.add_argument("--skewed-points", type=int, default=50_000_000, help="skewed 2-D workload size (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

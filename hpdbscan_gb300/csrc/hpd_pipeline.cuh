@@ -185,7 +185,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     need += dense_ok ? (size_t)g.total * 4 : 0;                      // dense cell lookup
     need += (size_t)d * n * 4;                                       // cell grid coordinates
     need += (size_t)n * 8;                                           // items
-    need += (size_t)n + 5 * (size_t)n * 4;                           // core, tmax, parent, broot, lm1, amb
+    need += (size_t)n + 6 * (size_t)n * 4;                           // core, tmax, tlow, parent, broot, lm1, amb
     need += (size_t)n * 4 + (size_t)n;                               // cell rep, cell flags
     need += 9 * (size_t)n * 4;                                       // dirty / schedule stamps, dirty list, work lists, cell / item min, item flags
     // dense cells: sub-cells per dimension (0: path off), see k_dense_assign
@@ -235,6 +235,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     int2* items = main.take<int2>(n);
     uint8_t* core = main.take<uint8_t>(n);
     int* tmax = main.take<int>(n);
+    int* tlow = main.take<int>(n);
     int* parent = main.take<int>(n);
     int* broot = main.take<int>(n);
     int* lm1 = main.take<int>(n);
@@ -340,6 +341,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     a.amb = amb;
     a.n_amb = flags_dev + 0;
     a.tmax = tmax;
+    a.tlow = tlow;
     a.lm1 = lm1;
     a.changed = flags_dev + 1;
     a.cellrank = rank;
@@ -489,6 +491,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
             a.amb = lists[cur];
             a.n_amb = counts[cur];
             HPD_CU(cudaMemsetAsync(tmax, 0xff, (size_t)n * sizeof(int), s));
+            HPD_CU(cudaMemsetAsync(tlow, 0x7f, (size_t)n * sizeof(int), s));  // 0x7f7f7f7f: no threshold yet
             HPD_QUERY_DISPATCH(k_tie_mark, T, mode, d, blocks_for(h_left, 4), 128, 0, s, a);
             info.launches += 1;
             if (round == 0 && d <= 5) {
@@ -564,6 +567,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 a.amb = lists[cur];
                 a.n_amb = counts[cur];
                 HPD_CU(cudaMemsetAsync(tmax, 0xff, (size_t)n * sizeof(int), s));
+                HPD_CU(cudaMemsetAsync(tlow, 0x7f, (size_t)n * sizeof(int), s));
                 HPD_QUERY_DISPATCH(k_tie_mark, T, mode, d, blocks_for(h_left, 4), 128, 0, s, a);
                 info.launches += 1;
             }

@@ -174,6 +174,7 @@ struct QueryArgs {
     int* amb;             // ambiguous border points
     int* n_amb;
     int* tmax;            // per root: highest position of a core next to an undecided border
+    int* tlow;            // per root: a value below it decides every undecided border of the component
                           // (-1: component not involved); only positions <= tmax matter
     int* lm1;             // tie-break value L - 1 (see k_tie_edge)
     int* changed;
@@ -1125,8 +1126,33 @@ __global__ void __launch_bounds__(128) k_tie_mark(QueryArgs<T> a) {
     if (w >= *a.n_amb) return;
     const int b = a.amb[w];
     if (!in_range(a.guard, b, a.n, kGuardAmbiguous)) return;
+    // r1 < r2: the two smallest roots next to b
+    int r1 = INT_MAX, r2 = INT_MAX;
     scan_point<T, M, D>(a, b, [&](int j) {
-        if (in_range(a.guard, a.parent[j], a.n, kGuardRoot)) atomicMax(a.tmax + a.parent[j], j);
+        const int x = a.parent[j];
+        if (!in_range(a.guard, x, a.n, kGuardRoot)) return;
+        atomicMax(a.tmax + x, j);
+        if (x < r1) {
+            r2 = r1;
+            r1 = x;
+        } else if (x != r1 && x < r2) {
+            r2 = x;
+        }
+    });
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const int b1 = __shfl_xor_sync(0xffffffffu, r1, o), b2 = __shfl_xor_sync(0xffffffffu, r2, o);
+        const int n1 = min(r1, b1);
+        const int n2 = r1 == b1 ? min(r2, b2) : (r1 < b1 ? min(r2, b1) : min(b2, r1));
+        r1 = n1;
+        r2 = n2;
+    }
+    // The component of r1 wins b as soon as one of its cores next to b holds a value
+    // below r2 (every other value is at least r2), so its values need no improvement
+    // below r2; every other component's values must be exact (threshold root + 1).
+    scan_point<T, M, D>(a, b, [&](int j) {
+        const int x = a.parent[j];
+        if (in_range(a.guard, x, a.n, kGuardRoot)) atomicMin(a.tlow + x, x == r1 ? r2 : x + 1);
     });
 }
 
@@ -1171,9 +1197,14 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
     const int p = it.y + (int)lane_id();
     bool active = p < pend && a.core[p];
     const int root = active ? a.parent[p] : INT_MIN;
-    // a core whose value is its component root holds the smallest value possible
     if (active && !in_range(a.guard, root, a.n, kGuardRoot)) active = false;
-    if (active) active = p <= a.tmax[root] && ld_volatile(a.lm1 + p) > root;
+    // a core whose value is below its component's threshold (at least root + 1: the
+    // root is the smallest value possible) needs no further improvement
+    int tl = INT_MIN;
+    if (active) {
+        tl = a.tlow[root];
+        active = p <= a.tmax[root] && ld_volatile(a.lm1 + p) >= tl;
+    }
     if (!__any_sync(0xffffffffu, active)) return;
     if (a.trace_counts) {
         const unsigned am = __ballot_sync(0xffffffffu, active);  // every lane takes part
@@ -1202,8 +1233,8 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
         return better;
     };
     auto never = []() { return false; };
-    // a lane is finished once its value is its component root
-    auto settled = [&]() { return __all_sync(0xffffffffu, !active || myl <= root); };
+    // a lane is finished once its value is below its component's threshold
+    auto settled = [&]() { return __all_sync(0xffffffffu, !active || myl < tl); };
     // tiles are aligned with the 32-point chunks of a cell, so each tile is one work
     // item; a tile whose smallest value cannot improve any lane is skipped unread
     auto scan_pruned = [&](int cr, int cs, int ce, int worst) {
@@ -1228,7 +1259,7 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
             const bool improved = publish();
             if (!own_dirty && !__any_sync(0xffffffffu, improved)) return true;
             if (!settled()) {
-                int worst = (active && myl > root) ? myl : INT_MIN;
+                int worst = (active && myl >= tl) ? myl : INT_MIN;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
                 scan_pruned(r, a.ct.start[r], it.y, worst);
@@ -1248,7 +1279,7 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
         if ((a.cell_flags[cr] & kCellUniform) && tmax_of(a, rep_c) < a.ct.start[cr]) return true;
         // no core of that cell holds a value below any lane's: nothing to gain
         if (settled()) return true;
-        int worst = (active && myl > root) ? myl : INT_MIN;
+        int worst = (active && myl >= tl) ? myl : INT_MIN;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
         if (ld_volatile(a.cell_min_l + cr) >= worst) return true;
