@@ -344,6 +344,45 @@ __device__ __forceinline__ bool scan_dense(const QueryArgs<T>& a, const Tile<T>&
     return false;
 }
 
+// Like scan_range for union-find work, with the expensive per-candidate lookup done
+// lazily: each lane first tests its query against the tile's core candidates
+// (test(q, u)), and aux_of runs only for candidates that some lane hit (one lane per
+// candidate); on_hit(q, u, aux) then runs per lane for its own hits.
+template <typename T, class Test, class Aux, class OnHit, class Done>
+__device__ __forceinline__ bool scan_range_hits(const QueryArgs<T>& a, const Tile<T>& tile, int cs, int ce, Test&& test,
+                                                Aux&& aux_of, OnHit&& on_hit, Done&& done) {
+    const int d = a.g.d;
+    const int S = tile_stride(d);
+    const unsigned lane = lane_id();
+    for (int t0 = cs; t0 < ce; t0 += 32) {
+        const int j = t0 + (int)lane;
+        bool is_core = false;
+        if (j < ce) {
+            for (int k = 0; k < d; ++k) tile.c[lane * S + k] = a.coords[(size_t)k * a.n + j];
+            is_core = a.core[j] != 0;
+        }
+        const unsigned cores = __ballot_sync(0xffffffffu, is_core);
+        __syncwarp();
+        unsigned mine = 0;
+        for (unsigned m = cores; m; m &= m - 1) {
+            const int u = __ffs(m) - 1;
+            if (test(t0 + u, u)) mine |= 1u << u;
+        }
+        const unsigned hit = __reduce_or_sync(0xffffffffu, mine);
+        if (hit) {
+            if ((hit >> lane) & 1u) tile.aux[lane] = aux_of(j);
+            __syncwarp();
+            for (; mine; mine &= mine - 1) {
+                const int u = __ffs(mine) - 1;
+                on_hit(t0 + u, u, tile.aux[u]);
+            }
+        }
+        __syncwarp();
+        if (done()) return true;
+    }
+    return false;
+}
+
 // candidate u of the tile into c[] (vector loads for d = 2..4)
 template <typename T, int D>
 __device__ __forceinline__ void tile_load(const Tile<T>& tile, int u, int d, T* c) {
@@ -574,16 +613,15 @@ __global__ void __launch_bounds__(128) k_union_intra(QueryArgs<T> a) {
     T q[D > 0 ? D : kMaxDims];
     load_query<T, D>(a, p, active, q);
     int myroot = active ? uf_find(a.parent, p) : -1;
-    auto aux_of = [&](int j) { return a.core[j] ? uf_find(a.parent, j) : -1; };
-    auto pair = [&](int qi, int u, int rep) {
-        if (!active || rep < 0 || rep == myroot || qi >= p) return;
-        if (within<T, M, D>(a, q, tile, u)) {
-            uf_union(a.parent, p, qi);
-            myroot = uf_find(a.parent, p);
-        }
+    auto test = [&](int qi, int u) { return active && qi < p && within<T, M, D>(a, q, tile, u); };
+    auto aux_of = [&](int j) { return uf_find(a.parent, j); };
+    auto on_hit = [&](int qi, int, int rep) {
+        if (rep == myroot) return;
+        uf_union(a.parent, p, qi);
+        myroot = uf_find(a.parent, p);
     };
     auto never = []() { return false; };
-    scan_range(a, tile, a.ct.start[r], pend, aux_of, pair, never);
+    scan_range_hits(a, tile, a.ct.start[r], pend, test, aux_of, on_hit, never);
 }
 
 static __global__ void k_cell_rep(const uint8_t* core, int* parent, const uint32_t* cellrank, int n, int* cell_rep) {
@@ -966,13 +1004,12 @@ __global__ void __launch_bounds__(128) k_union_cross(QueryArgs<T> a) {
     int myroot = active ? uf_find(a.parent, p) : -1;
     const bool uni_r = (a.cell_flags[r] & kCellUniform) != 0;
     const int rep_r = a.cell_rep[r];
-    auto aux_of = [&](int j) { return a.core[j] ? uf_find(a.parent, j) : -1; };
-    auto pair = [&](int qi, int u, int rep) {
-        if (!active || rep < 0 || rep == myroot) return;
-        if (within<T, M, D>(a, q, tile, u)) {
-            uf_union(a.parent, p, qi);
-            myroot = uf_find(a.parent, p);
-        }
+    auto test = [&](int, int u) { return active && within<T, M, D>(a, q, tile, u); };
+    auto aux_of = [&](int j) { return uf_find(a.parent, j); };
+    auto on_hit = [&](int qi, int, int rep) {
+        if (rep == myroot) return;
+        uf_union(a.parent, p, qi);
+        myroot = uf_find(a.parent, p);
     };
     visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
         if (own) return true;
@@ -981,7 +1018,7 @@ __global__ void __launch_bounds__(128) k_union_cross(QueryArgs<T> a) {
         const bool both = uni_r && (a.cell_flags[cr] & kCellUniform);
         if (both && same_component(a.parent, rep_r, rep_c)) return true;
         auto done = [&]() { return both && same_component(a.parent, rep_r, rep_c); };
-        scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
+        scan_range_hits(a, tile, a.ct.start[cr], a.ct.start[cr + 1], test, aux_of, on_hit, done);
         return true;
     }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore; });
 }
@@ -1418,7 +1455,11 @@ __global__ void __launch_bounds__(128) k_tie_greedy(QueryArgs<T> a) {
     const int pend = min(it.y + 32, a.ct.start[r + 1]);
     const int p = it.y + (int)lane_id();
     bool active = p < pend && a.core[p];
-    if (active) active = p <= a.tmax[a.parent[p]];
+    if (active) {
+        // positions below the component's threshold are settled already (value p)
+        const int root = a.parent[p];
+        active = p <= a.tmax[root] && p >= a.tlow[root];
+    }
     if (!__any_sync(0xffffffffu, active)) return;
     const Tile<T> tile = warp_tile<T>(a.g.d);
     T q[D > 0 ? D : kMaxDims];
