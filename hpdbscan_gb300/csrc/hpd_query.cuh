@@ -1023,11 +1023,22 @@ __global__ void __launch_bounds__(128) k_union_cross(QueryArgs<T> a) {
     }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore; });
 }
 
-// every core points at its component root; counts the cores (one atomic per warp)
+// Every core points at its component root; counts the cores (one atomic per warp).
+// The walk to the root only reads, so the only value ever written is a root: a
+// path-halving find here could overwrite another thread's root with a stale
+// grandparent and leave a core pointing below its root.
 static __global__ void k_compress(int* parent, const uint8_t* core, int n, int* n_core) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool c = i < n && core[i];
-    if (c) parent[i] = uf_find(parent, i);
+    if (c) {
+        int x = i;
+        for (;;) {  // parents strictly decrease along the walk, so it ends
+            const int up = ld_volatile(parent + x);
+            if (up == x) break;
+            x = up;
+        }
+        parent[i] = x;
+    }
     const unsigned m = __ballot_sync(0xffffffffu, c);
     if (lane_id() == 0 && m) atomicAdd(n_core, __popc(m));
 }

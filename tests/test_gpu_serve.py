@@ -72,3 +72,20 @@ def test_server_rejects_bad_job(gpu):
     with Server(workers=1) as srv:
         with pytest.raises(ValueError, match="epsilon"):
             srv.submit(np.zeros((10, 2), np.float32), -1.0, 3)
+
+
+def test_batch_large_instances_identical_and_repeatable(gpu):
+    """Instances of up to 1M points (dense cells, deep union-find trees): concurrent batch
+    labels equal standalone labels, and standalone labels are the same run to run."""
+    from hpdbscan_gb300 import workloads
+    from hpdbscan_gb300.serve import cluster_batch
+    items = []
+    for i in range(48):
+        w = workloads.batch_instance(i)
+        items.append((w.points, w.eps, w.min_points))
+    got = cluster_batch(items, workers=8)
+    want = _alone(items)
+    again = _alone(items)
+    for k, (g, w, w2) in enumerate(zip(got, want, again)):
+        assert np.array_equal(w, w2), k
+        assert np.array_equal(g, w), k
