@@ -418,9 +418,10 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     k_fill_int<<<blocks_for(m, 256), 256, 0, s>>>(cell_rep, m, kNoCore);
     k_cell_rep<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep);
     k_cell_uniform<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep, cell_flags);
+    HPD_QUERY_DISPATCH(k_union_cells, T, mode, d, blocks_for(m, 4), 128, 0, s, a);
     HPD_QUERY_DISPATCH(k_union_cross, T, mode, d, qgrid, 128, qsmem, s, a);
     k_compress<<<blocks_for(n, 256), 256, 0, s>>>(parent, core, n, flags_dev + 6);
-    info.launches += 7;
+    info.launches += 8;
     if (timed) HPD_CU(cudaEventRecord(tm->ev[3], s));
 
     // ---- borders

@@ -1011,16 +1011,70 @@ __global__ void __launch_bounds__(128) k_union_cross(QueryArgs<T> a) {
         uf_union(a.parent, p, qi);
         myroot = uf_find(a.parent, p);
     };
+    (void)rep_r;
+    // pairs of single-component cells are joined by k_union_cells
     visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
         if (own) return true;
-        const int rep_c = a.cell_rep[cr];
-        if (rep_c == kNoCore) return true;
-        const bool both = uni_r && (a.cell_flags[cr] & kCellUniform);
-        if (both && same_component(a.parent, rep_r, rep_c)) return true;
-        auto done = [&]() { return both && same_component(a.parent, rep_r, rep_c); };
-        scan_range_hits(a, tile, a.ct.start[cr], a.ct.start[cr + 1], test, aux_of, on_hit, done);
+        auto never = []() { return false; };
+        scan_range_hits(a, tile, a.ct.start[cr], a.ct.start[cr + 1], test, aux_of, on_hit, never);
         return true;
-    }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore; });
+    }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore && !(uni_r && (a.cell_flags[cr] & kCellUniform)); });
+}
+
+// Cross-cell unions between single-component cells, one warp per cell: for each
+// lower neighbour cell that is also single-component and not yet in the same
+// component, the lanes take 32 cores of the cell at a time and stream the
+// neighbour's cores past them until one core-core eps pair is found, which joins the
+// two components (a single pair suffices).
+template <typename T, int M, int D>
+__global__ void __launch_bounds__(128) k_union_cells(QueryArgs<T> a) {
+    const int c = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (c >= a.ct.m) return;
+    const int rep_c = a.cell_rep[c];
+    if (rep_c == kNoCore || !(a.cell_flags[c] & kCellUniform)) return;
+    const unsigned lane = lane_id();
+    const int d = a.g.d;
+    const int cs = a.ct.start[c], ce = a.ct.start[c + 1];
+    visit_stencil(a.g, a.ct, c, 1, [&](int cr, bool own) {
+        if (own) return true;
+        const int rep_n = a.cell_rep[cr];
+        if (same_component(a.parent, rep_c, rep_n)) return true;
+        const int ns = a.ct.start[cr], ne = a.ct.start[cr + 1];
+        bool joined = false;
+        for (int x0 = cs; x0 < ce && !joined; x0 += 32) {
+            const int x = x0 + (int)lane;
+            const bool ca = x < ce && a.core[x];
+            if (!__any_sync(0xffffffffu, ca)) continue;
+            T qa[D > 0 ? D : kMaxDims];
+            load_query<T, D>(a, x, ca, qa);
+            for (int y0 = ns; y0 < ne && !joined; y0 += 32) {
+                const int y = y0 + (int)lane;
+                const bool cb = y < ne && a.core[y];
+                T vb[D > 0 ? D : kMaxDims];
+                load_query<T, D>(a, y, cb, vb);
+                unsigned cand = __ballot_sync(0xffffffffu, cb);
+                while (cand) {
+                    const int u = __ffs(cand) - 1;
+                    cand &= cand - 1;
+                    T cu[D > 0 ? D : kMaxDims];
+#pragma unroll
+                    for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                        if (D == 0 && k >= d) break;
+                        cu[k] = shfl_val(vb[k], u);
+                    }
+                    const unsigned hit = __ballot_sync(0xffffffffu, ca && within_vals<T, M, D>(a, qa, cu));
+                    if (hit) {
+                        const int xa = x0 + __ffs(hit) - 1;
+                        if (lane == 0) uf_union(a.parent, xa, y0 + u);
+                        __syncwarp();
+                        joined = true;
+                        break;
+                    }
+                }
+            }
+        }
+        return true;
+    }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore && (a.cell_flags[cr] & kCellUniform); });
 }
 
 // Every core points at its component root; counts the cores (one atomic per warp).
