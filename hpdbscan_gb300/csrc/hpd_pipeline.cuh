@@ -198,7 +198,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         for (int kk = 2; kk <= 3 && !dense_k; ++kk) {
             int groups = 1;
             for (int k = 0; k < d; ++k) groups *= kk;
-            if (groups <= 81 && std::sqrt((double)d) * ((double)rq.eps / kk + 4 * err) <= 0.95 * (double)rq.eps)
+            if (groups <= kDenseMaxGroups && std::sqrt((double)d) * ((double)rq.eps / kk + 4 * err) <= 0.95 * (double)rq.eps)
                 dense_k = kk;
         }
     }

@@ -54,12 +54,6 @@ __device__ __forceinline__ int find_cell(const CellTable& ct, unsigned long long
     return (lo < ct.m && ct.key[lo] == key) ? lo : -1;
 }
 
-template <typename T>
-__device__ __forceinline__ T shfl_xor_val(T v, int mask) {
-    if constexpr (sizeof(T) < 4) return (T)__shfl_xor_sync(0xffffffffu, (int)v, mask);
-    else return __shfl_xor_sync(0xffffffffu, v, mask);
-}
-
 // Warp-aggregated atomics: the lanes of a warp that target the same address combine
 // their values first, so that cells of millions of points cost one atomic per warp
 // rather than one per point.  Every lane of the warp must call; lanes with ok false
@@ -868,23 +862,6 @@ __global__ void __launch_bounds__(128) k_mark_near_big(QueryArgs<T> a, DenseArgs
         if (lane_id() == 0) a.cell_flags[cr] |= kCellNearBig;
         return true;
     });
-}
-
-template <typename T, int M, int D>
-__device__ __forceinline__ bool within_pts(const QueryArgs<T>& a, int i, int j) {
-    if constexpr (!Elem<T>::kFloat) {
-        T x[D > 0 ? D : kMaxDims], y[D > 0 ? D : kMaxDims];
-        for (int k = 0; k < a.g.d; ++k) { x[k] = a.coords[(size_t)k * a.n + i]; y[k] = a.coords[(size_t)k * a.n + j]; }
-        return int_within<T, D>(x, y, a.g.d, a.eps2);
-    } else {
-        T t[D > 0 ? D : kMaxDims];
-#pragma unroll
-        for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-            if (D == 0 && k >= a.g.d) break;
-            t[k] = sub_(a.coords[(size_t)k * a.n + i], a.coords[(size_t)k * a.n + j]);
-        }
-        return fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
-    }
 }
 
 __device__ __forceinline__ bool same_component(int* parent, int x, int y);
