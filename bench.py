@@ -55,6 +55,23 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def slowest_rank(seconds, world, device="cpu"):
+    """Time of the slowest replica: every rank clusters its own copy of the workload,
+    so the job is done when the last rank is (all-reduce MAX; identity at N = 1)."""
+    if world <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_mpoints_per_s(points_per_rank, steps, world, slowest_seconds):
+    """Whole-job throughput of N replicas: N x points x steps / the slowest rank's time."""
+    return world * points_per_rank * steps / slowest_seconds / 1e6
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -347,13 +364,10 @@ def run_engine(args):
             launches += int(st["kernel_launches"])
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
-    total_ms = sum(step_ms)
+    total_ms = 1000 * slowest_rank(sum(step_ms) / 1000, world, "cuda")
     if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
         torch.distributed.barrier()
-    value = world * n * args.steps / (total_ms / 1000) / 1e6
+    value = job_mpoints_per_s(n, args.steps, world, total_ms / 1000)
 
     # end to end through the host-buffer entry point (pinned input, labels back to host)
     progress("host-buffer steps")
@@ -377,12 +391,8 @@ def run_engine(args):
         t0 = time.perf_counter()
         e2e_step()
         e2e_s.append(time.perf_counter() - t0)
-    e2e_total = sum(e2e_s)
-    if world > 1:
-        t = torch.tensor([e2e_total], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * n * args.steps / e2e_total / 1e6
+    e2e_total = slowest_rank(sum(e2e_s), world, "cuda")
+    e2e_value = job_mpoints_per_s(n, args.steps, world, e2e_total)
     same = bool(torch.equal(host_labels.cuda(), labels))
 
     if rank != 0:
