@@ -343,8 +343,9 @@ def run_engine(args):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    clock = Clock(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv") if os.path.isdir(
-        os.path.join(ROOT, "gpurun_out")) else f"/tmp/hpd_clocks_{os.getpid()}.csv")
+    # nvidia-smi samples of the timed region (directory: HPD_BENCH_OUT, else the temp dir)
+    import tempfile
+    clock = Clock(os.path.join(os.environ.get("HPD_BENCH_OUT", tempfile.gettempdir()), f"hpd_clocks_rank{rank}.csv"))
     step_ms, core_ms, phases = [], [], []
     launches = 0
     progress("device-resident steps")
