@@ -135,18 +135,34 @@ __global__ void k_minmax_partial(const T* __restrict__ data, int64_t count, int 
 }
 
 template <typename T>
-__global__ void k_minmax_final(const T* __restrict__ pmin, const T* __restrict__ pmax, int nblocks, int d,
-                               T* __restrict__ out /* [2d]: mins, maxs */) {
-    const int k = threadIdx.x;
-    if (k >= d) return;
-    T mn = Elem<T>::highest(), mx = Elem<T>::lowest();
-    for (int b = 0; b < nblocks; ++b) {
-        T a = pmin[(int64_t)b * d + k], c = pmax[(int64_t)b * d + k];
-        if (a < mn) mn = a;
-        if (mx < c) mx = c;
+__global__ void __launch_bounds__(256) k_minmax_final(const T* __restrict__ pmin, const T* __restrict__ pmax, int nblocks,
+                                                      int d, T* __restrict__ out /* [2d]: mins, maxs */) {
+    // one block of 256 threads: every thread folds a strided share of the partial
+    // results of each dimension, then a tree in shared memory (min / max are exact)
+    __shared__ T smn[256], smx[256];
+    for (int k = 0; k < d; ++k) {
+        T mn = Elem<T>::highest(), mx = Elem<T>::lowest();
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+            const T a = pmin[(int64_t)b * d + k], c = pmax[(int64_t)b * d + k];
+            if (a < mn) mn = a;
+            if (mx < c) mx = c;
+        }
+        smn[threadIdx.x] = mn;
+        smx[threadIdx.x] = mx;
+        __syncthreads();
+        for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+            if ((int)threadIdx.x < h) {
+                if (smn[threadIdx.x + h] < smn[threadIdx.x]) smn[threadIdx.x] = smn[threadIdx.x + h];
+                if (smx[threadIdx.x] < smx[threadIdx.x + h]) smx[threadIdx.x] = smx[threadIdx.x + h];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            out[k] = smn[0];
+            out[d + k] = smx[0];
+        }
+        __syncthreads();
     }
-    out[k] = mn;
-    out[d + k] = mx;
 }
 
 // ------------------------------------------------------------- cell ids
@@ -232,7 +248,8 @@ static __global__ void k_item_flags(const uint32_t* __restrict__ cellrank, const
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if ((threadIdx.x & 31) == 0 && v) atomicMax(max_cell, v);
+    // the maximum settles early, so most warps only read it (no contended atomic)
+    if ((threadIdx.x & 31) == 0 && v && v > *(volatile uint32_t*)max_cell) atomicMax(max_cell, v);
 }
 
 static __global__ void k_item_write(const uint32_t* __restrict__ item_flag, const uint32_t* __restrict__ item_pos,

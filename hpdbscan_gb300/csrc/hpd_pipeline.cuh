@@ -107,7 +107,7 @@ int run_pipeline(const Request& rq, Arena& small, Arena& main, Timers* tm, RunIn
     }
     HPD_CU(cudaMemsetAsync(bad, 0, sizeof(int), s));
     k_minmax_partial<T><<<nblk, tpb, 2 * tpb * sizeof(T), s>>>(static_cast<const T*>(rq.d_data), count, d, pmin, pmax, bad);
-    k_minmax_final<T><<<1, 32, 0, s>>>(pmin, pmax, nblk, d, ext);
+    k_minmax_final<T><<<1, 256, 0, s>>>(pmin, pmax, nblk, d, ext);
     info.launches += 2;
     if (tm && tm->ok) HPD_CU(cudaEventRecord(tm->ev[7], s));
     T h_ext[2 * kMaxDims];
