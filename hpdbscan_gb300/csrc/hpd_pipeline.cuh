@@ -76,6 +76,7 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
 
 constexpr int kDenseMinPoints = 128;  // cells with this many points take the dense-cell path
 constexpr int kFineMinPoints = 65536;  // a largest cell this big selects the finer sub-cell split
+constexpr int kJumpPasses = 8;          // relaxation passes followed by a pointer-jumping sweep
 
 template <typename T, typename K>
 int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, std::string& err, const Grid& g,
@@ -530,7 +531,9 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 if (trace) HPD_CU(cudaMemsetAsync(tcount, 0, 2 * sizeof(unsigned long long), s));
                 if (pass == 1) HPD_QUERY_DISPATCH(k_tie_edge, T, mode, d, qgrid, 128, qsmem, s, a);
                 else HPD_QUERY_DISPATCH(k_tie_edge_list, T, mode, d, list_grid, 128, qsmem, s, a);
-                k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
+                // pointer jumping speeds up the early passes; in the tail few values change
+                // and the edge passes alone reach the same (exact) fixpoint
+                if (pass <= kJumpPasses) k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
                 k_tie_schedule<T><<<list_grid, 128, 0, s>>>(a);
                 exclusive_scan<uint32_t>(item_flag, item_pos, n_items, scan32,
                                          reinterpret_cast<uint32_t*>(a.n_wlist_out), s, &info.launches);
