@@ -25,6 +25,9 @@ Sets:
   int_<type>_d{2,3}  the eight integer element types (upstream instantiations), with
                      coordinates and eps chosen so that the squared distances wrap
                      around and EPS2 overflows the narrow types
+  big_cells_d{2,3}   compact blobs (sigma eps/20) in cells of up to ~70,000 points,
+                     ringed by points at every distance: cells this full take the
+                     box-pruned queries and the finer sub-cell split
 """
 from __future__ import annotations
 
@@ -108,6 +111,19 @@ def kat_cells(seed: int = 5):
     return pts, float(eps)
 
 
+def big_cells(d: int, seed: int):
+    """A blob of 70,000 points with sigma eps/20 (one cell holds most of it), smaller
+    compact blobs, a ring of points within 3 eps of every centre and uniform noise."""
+    rng = np.random.default_rng(seed)
+    eps = 0.01
+    centres = rng.random((4, d)) * 0.5 + 0.25
+    blobs = [centres[0] + rng.normal(0, eps / 20, (70000, d))]
+    blobs += [c + rng.normal(0, eps * 0.2, (int(rng.integers(3000, 9000)), d)) for c in centres[1:]]
+    ring = np.concatenate([c + rng.uniform(-3 * eps, 3 * eps, (1500, d)) for c in centres])
+    pts = np.concatenate(blobs + [ring, rng.random((2000, d))]).astype(np.float32)
+    return pts[rng.permutation(len(pts))], eps
+
+
 def main():
     if not po.ref_available():
         po.build(ref=True)
@@ -152,6 +168,9 @@ def main():
             c = rng.integers(lo, hi, (8, d))
             pts = np.clip(c[rng.integers(0, 8, 3000)] + rng.normal(0, eps, (3000, d)), lo, hi).astype(dt)
             save(f"int_{np.dtype(dt).name}_d{d}", pts, eps, 6)
+    for d in (2, 3):
+        pts, eps = big_cells(d, seed=60 + d)
+        save(f"big_cells_d{d}", pts, eps, 40)
     manifest = {
         "reference_build": "upstream include/*.h via oracle/Makefile: g++ -std=c++11 -Ofast -fopenmp",
         "compiler": subprocess.run(["g++", "--version"], capture_output=True, text=True).stdout.splitlines()[0],
