@@ -1,0 +1,122 @@
+// Core test: neighbour counts with an early exit at minPoints.
+#pragma once
+
+#include "hpd_query.cuh"
+
+namespace hpd {
+
+// ---------------------------------------------------------------- core test
+// |N_eps(p)| >= minPoints, self included, with an early exit once every query of
+// the warp has reached minPoints (hpdbscan.h:74-78).
+template <typename T>
+__device__ __forceinline__ T shfl_val(T v, int src) {
+    if constexpr (sizeof(T) < 4) return (T)__shfl_sync(0xffffffffu, (int)v, src);
+    else return __shfl_sync(0xffffffffu, v, src);
+}
+
+constexpr int kSparseQueries = 8;  // items with at most this many points use candidate lanes
+constexpr int kMaxRanges = 32;     // neighbour ranges kept in shared memory (3^d <= 32: d <= 3)
+
+template <typename T, int M, int D, bool PRUNE>
+__global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
+    __shared__ int2 s_rng[4][kMaxRanges];
+    const int w = threadIdx.x >> 5;
+    const int item = blockIdx.x * 4 + w;
+    if (item >= a.n_items) return;
+    const int2 it = a.items[item];
+    const int r = it.x;
+    // cells next to a big dense cell are handled by the PRUNE instantiation
+    if (((a.cell_flags[r] & kCellNearBig) != 0) != PRUNE) return;
+    const Tile<T> tile = warp_tile<T>(a.g.d);
+    const int pend = min(it.y + 32, a.ct.start[r + 1]);
+    const int p = it.y + (int)lane_id();
+    const bool active = p < pend;
+    T q[D > 0 ? D : kMaxDims];
+    load_query<T, D>(a, p, active, q);
+    int count = 0;
+    const int limit = a.min_points;
+    if (a.dense_id) {
+        // a point of a dense cell whose sub-cell holds >= minPoints points has that many
+        // neighbours within eps already (sub-cells are certified cliques)
+        const int id = a.dense_id[r];
+        if (id >= 0 && active) {
+            const int g = a.dense_gidx[p];
+            const int* grp = a.dense_grp + (size_t)id * (a.dense_groups + 1);
+            if (grp[g + 1] - grp[g] >= limit) count = limit;
+        }
+        if (__all_sync(0xffffffffu, !active || count >= limit)) {
+            if (active) a.core[p] = 1;
+            return;
+        }
+    }
+    int S = 1;
+    for (int sd = 0; sd < a.g.d; ++sd) S *= 3;
+    if (!PRUNE && pend - it.y <= kSparseQueries && S <= kMaxRanges) {
+        // few queries: the whole warp tests consecutive candidates of one query at a
+        // time (a ballot counts the hits), instead of leaving most lanes idle
+        int nr = 0;
+        visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
+            if (lane_id() == 0) s_rng[w][nr] = make_int2(a.ct.start[cr], a.ct.start[cr + 1]);
+            ++nr;
+            return true;
+        });
+        __syncwarp();
+        for (int src = 0; src < pend - it.y; ++src) {
+            T qq[D > 0 ? D : kMaxDims];
+#pragma unroll
+            for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                if (D == 0 && k >= a.g.d) break;
+                qq[k] = shfl_val(q[k], src);
+            }
+            int hits = 0;
+            for (int ri = 0; ri < nr && hits < limit; ++ri) {
+                const int ce = s_rng[w][ri].y;
+                for (int j0 = s_rng[w][ri].x; j0 < ce && hits < limit; j0 += 32) {
+                    const int j = j0 + (int)lane_id();
+                    bool hit = false;
+                    if (j < ce) {
+                        T c[D > 0 ? D : kMaxDims];
+#pragma unroll
+                        for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                            if (D == 0 && k >= a.g.d) break;
+                            c[k] = a.coords[(size_t)k * a.n + j];
+                        }
+                        hit = within_vals<T, M, D>(a, qq, c);
+                    }
+                    hits += __popc(__ballot_sync(0xffffffffu, hit));
+                }
+            }
+            if (lane_id() == 0) a.core[it.y + src] = hits >= limit ? 1 : 0;
+        }
+        return;
+    }
+    auto aux_of = [](int) { return 0; };
+    auto pair = [&](int, int u, int) {
+        if (active && within<T, M, D>(a, q, tile, u)) ++count;
+    };
+    auto done = [&]() { return __all_sync(0xffffffffu, !active || count >= limit); };
+    visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
+        if constexpr (PRUNE) {
+            if (pruned_cell(a, cr)) {
+                // a sub-cell wholly within eps adds its population without a scan; only
+                // sub-cells crossing the eps sphere are streamed, for the lanes they cross
+                const int* grp = a.dense_grp + (size_t)a.dense_id[cr] * (a.dense_groups + 1);
+                int cur = kBoxFar;
+                auto visit_group = [&](int g, int cls) -> bool {
+                    cur = cls;
+                    if (cls == kBoxIn) count += grp[g + 1] - grp[g];
+                    return __any_sync(0xffffffffu, cls == kBoxEdge);
+                };
+                auto pair_edge = [&](int, int u, int) {
+                    if (cur == kBoxEdge && within<T, M, D>(a, q, tile, u)) ++count;
+                };
+                return !scan_dense<T, D>(a, tile, cr, q, active && count < limit, visit_group, aux_of, pair_edge,
+                                         done);
+            }
+        }
+        return !scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
+    });
+    if (active) a.core[p] = count >= limit ? 1 : 0;
+}
+
+}  // namespace hpd

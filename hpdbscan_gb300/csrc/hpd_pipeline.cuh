@@ -13,6 +13,11 @@
 #include "hpd_index.cuh"
 #include "hpd_internal.h"
 #include "hpd_query.cuh"
+#include "hpd_core.cuh"
+#include "hpd_union.cuh"
+#include "hpd_dense.cuh"
+#include "hpd_border.cuh"
+#include "hpd_tie.cuh"
 
 namespace hpd {
 
