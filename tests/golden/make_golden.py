@@ -25,6 +25,8 @@ Sets:
   int_<type>_d{2,3}  the eight integer element types (upstream instantiations), with
                      coordinates and eps chosen so that the squared distances wrap
                      around and EPS2 overflows the narrow types
+  dims_d1, dims_d8   one dimension (with a cell of ~12,000 points) and eight
+                     dimensions (the generic paths past d = 5)
   big_cells_d{2,3}   compact blobs (sigma eps/20) in cells of up to ~70,000 points,
                      ringed by points at every distance: cells this full take the
                      box-pruned queries and the finer sub-cell split
@@ -124,6 +126,21 @@ def big_cells(d: int, seed: int):
     return pts[rng.permutation(len(pts))], eps
 
 
+def dims_case(d: int, seed: int):
+    """Blob mixture in d dimensions; for d = 1 one blob is compact enough to fill a
+    single cell with ~12,000 points."""
+    rng = np.random.default_rng(seed)
+    eps = 0.0005 if d == 1 else 0.08
+    centres = rng.random((8, d))
+    sig = np.full(8, eps * 0.6)
+    n = [3000] * 8
+    if d == 1:
+        sig[0], n[0] = eps * 0.05, 12000
+    blobs = [c + rng.normal(0, s, (k, d)) for c, s, k in zip(centres, sig, n)]
+    pts = np.concatenate(blobs + [rng.random((2000, d))]).astype(np.float32)
+    return pts[rng.permutation(len(pts))], eps
+
+
 def main():
     if not po.ref_available():
         po.build(ref=True)
@@ -168,6 +185,9 @@ def main():
             c = rng.integers(lo, hi, (8, d))
             pts = np.clip(c[rng.integers(0, 8, 3000)] + rng.normal(0, eps, (3000, d)), lo, hi).astype(dt)
             save(f"int_{np.dtype(dt).name}_d{d}", pts, eps, 6)
+    for d in (1, 8):
+        pts, eps = dims_case(d, seed=70 + d)
+        save(f"dims_d{d}", pts, eps, 10)
     for d in (2, 3):
         pts, eps = big_cells(d, seed=60 + d)
         save(f"big_cells_d{d}", pts, eps, 40)
