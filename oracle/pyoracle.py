@@ -2,7 +2,8 @@
 
 * ``cluster``      -> oracle/_build/libhpdoracle.so, the C restatement (hpd_oracle.c)
 * ``ref_cluster``  -> oracle/_ref/libhpdref.so, the upstream headers compiled unmodified
-                      with the upstream flags (only where the upstream sources exist)
+                      with the upstream flags on this host (from the upstream checkout,
+                      or from the copy `make -C oracle stage` leaves in oracle/_ref/upstream)
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
 import this module.
@@ -18,7 +19,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libhpdoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libhpdref.so")
-REF_INCLUDE = os.environ.get("HPD_REF_INCLUDE", "/root/reference/include")
+REF_ROOT = os.environ.get("HPD_REF_ROOT", "/root/reference")
+REF_INCLUDE = os.path.join(REF_ROOT, "include")
+# the upstream headers staged unmodified by `make -C oracle stage` (git-ignored), so
+# that a host without the upstream checkout can build the reference from them
+REF_STAGED = os.path.join(HERE, "_ref", "upstream", "include")
 
 CELL_RECIP, CELL_DIV = 0, 1
 DIST_GCC_X86, DIST_SEQ, DIST_SEQ_FMA = 0, 1, 2
@@ -33,13 +38,21 @@ _lib = None
 _ref = None
 
 
+def ref_sources_available() -> bool:
+    return os.path.exists(os.path.join(REF_INCLUDE, "hpdbscan.h")) or \
+        os.path.exists(os.path.join(REF_STAGED, "hpdbscan.h"))
+
+
 def build(ref: bool | None = None) -> None:
-    """Compile the restatement (always) and the upstream build (when its sources exist)."""
+    """Compile the restatement (always) and the upstream build (when its sources exist:
+    the upstream checkout, which is then also staged, or a staged copy)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     if ref is None:
-        ref = os.path.isdir(REF_INCLUDE)
+        ref = ref_sources_available()
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_INCLUDE={REF_INCLUDE}"], check=True)
+        if os.path.exists(os.path.join(REF_INCLUDE, "hpdbscan.h")):
+            subprocess.run(["make", "-s", "-C", HERE, "stage", f"REF_ROOT={REF_ROOT}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={REF_ROOT}"], check=True)
 
 
 def _load():
