@@ -6,7 +6,6 @@
 #include <cuda_runtime.h>
 
 #include <climits>
-#include <mutex>
 #include <string>
 
 #include "hpd_internal.h"
@@ -16,12 +15,7 @@ namespace {
 constexpr int64_t kNoAllocMaxPoints = 32768;
 constexpr size_t kNoAllocSmallBytes = size_t(1) << 20;   // extent reduction partials
 constexpr size_t kNoAllocScratchBytes = size_t(16) << 20; // enough for 32768 points, d <= 16, doubles
-constexpr int kMaxDevices = 64;
-
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
-
-std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
 
 thread_local std::string g_err;
 
@@ -30,21 +24,19 @@ int fail(int code, const std::string& msg) {
     return code;
 }
 
-// Device address of the scratch array on the current device.  The array's name in
-// host code is only a host-side handle, so the address is looked up once per device
-// (with that device current) and cached.
-int scratch_address(int device, void** out) {
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_addr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            return fail(HPD_ERR_CUDA, std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
-        }
-        g_scratch_addr[device] = p;
+// Device address of the scratch array on the current device.  In host code the
+// array's name is only a host-side stand-in, so the address is looked up with the
+// device current.  The lookup runs on every call (it allocates nothing): an address
+// kept from an earlier call would go stale after cudaDeviceReset or under another
+// context on the same device, and kernels would then write through it.
+int scratch_address(void** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return fail(HPD_ERR_CUDA, std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
     }
-    *out = g_scratch_addr[device];
+    *out = p;
     return HPD_OK;
 }
 
@@ -70,12 +62,12 @@ int hpd_cluster_device_noalloc(float epsilon, uint64_t min_points, int32_t cell_
     if (n == 0) return HPD_OK;
     if (!d_data || !d_labels) return fail(HPD_ERR_INVALID, "null data or label pointer");
     int device = 0;
-    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) {
+    if (cudaGetDevice(&device) != cudaSuccess) {
         cudaGetLastError();
         return fail(HPD_ERR_CUDA, "no usable CUDA device");
     }
     void* base = nullptr;
-    int rc = scratch_address(device, &base);
+    int rc = scratch_address(&base);
     if (rc) return rc;
 
     // two arenas over the static array; they never allocate or free

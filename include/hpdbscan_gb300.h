@@ -162,9 +162,11 @@ const char* hpd_server_last_error(void);
  *   - at most 32768 points (any d <= 16, float32 or float64); larger inputs fail with
  *     HPD_ERR_INVALID;
  *   - data, labels and stream as for hpd_cluster_device (NULL stream = the legacy
- *     default stream); returns after the labels are written;
- *   - the first call on a device looks up the array's device address (a one-time
- *     set-up per device): make that first call before any stream capture;
+ *     default stream); the call reads counts back and synchronises that stream
+ *     before it returns, after the labels are written;
+ *   - each call looks up the array's device address on the current device
+ *     (cudaGetSymbolAddress, which allocates nothing), so the address stays right
+ *     after cudaDeviceReset;
  *   - every call uses the same array, which keeps the last call's contents: calls that
  *     overlap on the GPU (from two host threads or two streams) race;
  *   - errors are reported by hpd_noalloc_last_error(). */

@@ -34,6 +34,13 @@ def test_no_alloc_matches_regular_entry_point_twice(gpu):
     ]
     f64 = workloads.batch_instance(0, n_max=20_000)              # d = 5, as float64
     inputs = [(w.points, w.eps, w.min_points) for w in cases] + [(f64.points.astype(np.float64), f64.eps, f64.min_points)]
+    # the largest plans the 16 MiB array must hold, at exactly 32768 points: sixteen
+    # float64 dimensions whose grid needs 64-bit cell ids, and four float32 dimensions
+    # with one dense cell (sub-cell tables)
+    rng = np.random.default_rng(7)
+    inputs.append((rng.random((32768, 16)), 0.25, 4))
+    dense = np.concatenate([0.5 + rng.standard_normal((30000, 4)) * 0.0025, rng.random((2768, 4))])
+    inputs.append((np.ascontiguousarray(dense, dtype=np.float32), 0.05, 8))
     for pts, eps, mp in inputs:
         assert len(pts) <= 32768
         x, want = _regular(torch, pts, eps, mp)
