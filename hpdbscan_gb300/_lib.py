@@ -17,8 +17,11 @@ F32, F64, I8, I16, I32, I64, U8, U16, U32, U64 = range(10)
 CELL_RECIP, CELL_DIV = 0, 1
 DIST_GCC_X86, DIST_SEQ, DIST_SEQ_FMA = 0, 1, 2
 TIE_EXACT, TIE_SMALLEST_ID = 0, 1
+DIAG_COUNT_PAIRS = 1
+INJECT_FAIL_ALLOC = 1
 
-EXPORTS = ("hpd_create", "hpd_destroy", "hpd_set_arith", "hpd_set_tie_break", "hpd_cluster", "hpd_cluster_device",
+EXPORTS = ("hpd_create", "hpd_destroy", "hpd_set_arith", "hpd_set_tie_break", "hpd_set_tie_pass_limit",
+           "hpd_set_diagnostics", "hpd_debug_inject", "hpd_cluster", "hpd_cluster_device",
            "hpd_get_stats", "hpd_last_error", "hpd_version", "hpd_cluster_device_noalloc",
            "hpd_noalloc_last_error", "hpd_cluster_batch", "hpd_server_create", "hpd_server_submit",
            "hpd_server_poll", "hpd_server_wait", "hpd_server_destroy", "hpd_server_last_error")
@@ -29,7 +32,7 @@ class Job(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("n", ctypes.c_int64), ("d", ctypes.c_int32), ("dtype", ctypes.c_int32),
                 ("epsilon", ctypes.c_float), ("min_points", ctypes.c_uint64), ("cell_mode", ctypes.c_int32),
                 ("dist_mode", ctypes.c_int32), ("labels", ctypes.c_void_p), ("status", ctypes.c_int32),
-                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double)]
+                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("deadline_ms", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -38,7 +41,8 @@ class Stats(ctypes.Structure):
                 ("finalize_ms", ctypes.c_double),
                 ("n_cells", ctypes.c_int64), ("n_core", ctypes.c_int64), ("n_ambiguous", ctypes.c_int64),
                 ("tie_iterations", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
-                ("extent_ms", ctypes.c_double), ("cells_sort_ms", ctypes.c_double), ("cell_table_ms", ctypes.c_double)]
+                ("extent_ms", ctypes.c_double), ("cells_sort_ms", ctypes.c_double), ("cell_table_ms", ctypes.c_double),
+                ("cell_ids_ms", ctypes.c_double), ("rules_ms", ctypes.c_double), ("core_pairs", ctypes.c_int64)]
 
 
 _lib = None
@@ -68,6 +72,9 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.hpd_set_arith.restype = ctypes.c_int
     lib.hpd_set_tie_break.argtypes = [H, ctypes.c_int]
     lib.hpd_set_tie_break.restype = ctypes.c_int
+    for name in ("hpd_set_tie_pass_limit", "hpd_set_diagnostics", "hpd_debug_inject"):
+        getattr(lib, name).argtypes = [H, ctypes.c_int32]
+        getattr(lib, name).restype = ctypes.c_int
     lib.hpd_cluster.argtypes = [H, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                 ctypes.c_void_p]
     lib.hpd_cluster.restype = ctypes.c_int

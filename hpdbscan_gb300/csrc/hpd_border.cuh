@@ -70,7 +70,10 @@ __global__ void __launch_bounds__(128) k_border(QueryArgs<T> a) {
     }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore; });
     if (active) {
         a.broot[p] = r1;
-        if (multi) a.amb[atomicAdd(a.n_amb, 1)] = p;
+        if (multi) {
+            const int k = atomicAdd(a.n_amb, 1);
+            if (in_range(a.guard, k, a.n, kGuardList)) a.amb[k] = p;
+        }
     }
 }
 

@@ -17,6 +17,9 @@ struct hpd_handle {
     int cell_mode = HPD_CELL_RECIP;
     int dist_mode = HPD_DIST_GCC_X86;
     int tie_mode = HPD_TIE_EXACT;
+    int tie_pass_limit = kDefaultTiePassLimit;
+    int diag = 0;    // hpd_diag bits
+    int inject = 0;  // hpd_inject bits for the next call
     int device = 0;
     cudaStream_t stream = nullptr;
     Arena small, main, in_buf, out_buf;
@@ -64,6 +67,8 @@ int run(hpd_handle* h, const void* d_data, int64_t n, int32_t d, int32_t dtype, 
     rq.tie_mode = h->tie_mode;
     rq.d_labels = d_labels;
     rq.stream = s;
+    rq.tie_pass_limit = h->tie_pass_limit;
+    rq.count_pairs = (h->diag & HPD_DIAG_COUNT_PAIRS) != 0;
     std::string err;
     int rc;
     switch (dtype) {
@@ -81,6 +86,15 @@ int run(hpd_handle* h, const void* d_data, int64_t n, int32_t d, int32_t dtype, 
     }
     if (rc != HPD_OK) return fail(rc, err);
     return HPD_OK;
+}
+// the injected allocation failure hits the first arena of the call that must grow
+void arm_alloc_failure(hpd_handle* h) {
+    if (!(h->inject & HPD_INJECT_FAIL_ALLOC)) return;
+    h->inject &= ~HPD_INJECT_FAIL_ALLOC;
+    h->in_buf.fail_next = h->out_buf.fail_next = h->small.fail_next = h->main.fail_next = true;
+}
+void disarm_alloc_failure(hpd_handle* h) {
+    h->in_buf.fail_next = h->out_buf.fail_next = h->small.fail_next = h->main.fail_next = false;
 }
 }  // namespace
 
@@ -141,6 +155,27 @@ int hpd_set_tie_break(hpd_handle* h, int mode) {
     return HPD_OK;
 }
 
+int hpd_set_tie_pass_limit(hpd_handle* h, int32_t passes) {
+    if (!h) return fail(HPD_ERR_INVALID, "null handle");
+    if (passes < 0) return fail(HPD_ERR_INVALID, "pass limit must be >= 0");
+    h->tie_pass_limit = passes == 0 ? kDefaultTiePassLimit : passes;
+    return HPD_OK;
+}
+
+int hpd_set_diagnostics(hpd_handle* h, int32_t flags) {
+    if (!h) return fail(HPD_ERR_INVALID, "null handle");
+    if (flags & ~HPD_DIAG_COUNT_PAIRS) return fail(HPD_ERR_INVALID, "bad diagnostics flags");
+    h->diag = flags;
+    return HPD_OK;
+}
+
+int hpd_debug_inject(hpd_handle* h, int32_t what) {
+    if (!h) return fail(HPD_ERR_INVALID, "null handle");
+    if (what & ~HPD_INJECT_FAIL_ALLOC) return fail(HPD_ERR_INVALID, "bad injection");
+    h->inject |= what;
+    return HPD_OK;
+}
+
 int hpd_cluster_device(hpd_handle* h, const void* d_data, int64_t n, int32_t d, int32_t dtype, int64_t* d_labels,
                        void* stream) {
     if (!h) return fail(HPD_ERR_INVALID, "null handle");
@@ -150,7 +185,10 @@ int hpd_cluster_device(hpd_handle* h, const void* d_data, int64_t n, int32_t d, 
     if (!d_data || !d_labels) return fail(HPD_ERR_INVALID, "null data or label pointer");
     if (cudaSetDevice(h->device) != cudaSuccess) return fail(HPD_ERR_CUDA, "cudaSetDevice failed");
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : h->stream;
-    return run(h, d_data, n, d, dtype, d_labels, s);
+    arm_alloc_failure(h);
+    rc = run(h, d_data, n, d, dtype, d_labels, s);
+    disarm_alloc_failure(h);
+    return rc;
 }
 
 int hpd_cluster(hpd_handle* h, const void* data, int64_t n, int32_t d, int32_t dtype, int32_t threads,
@@ -164,13 +202,18 @@ int hpd_cluster(hpd_handle* h, const void* data, int64_t n, int32_t d, int32_t d
     if (cudaSetDevice(h->device) != cudaSuccess) return fail(HPD_ERR_CUDA, "cudaSetDevice failed");
     const size_t in_bytes = (size_t)n * d * dtype_size(dtype);
     const size_t out_bytes = (size_t)n * sizeof(int64_t);
+    arm_alloc_failure(h);
     cudaError_t e = h->in_buf.reserve(in_bytes);
     if (e == cudaSuccess) e = h->out_buf.reserve(out_bytes);
-    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? HPD_ERR_NOMEM : HPD_ERR_CUDA, cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        disarm_alloc_failure(h);
+        return fail(e == cudaErrorMemoryAllocation ? HPD_ERR_NOMEM : HPD_ERR_CUDA, cudaGetErrorString(e));
+    }
     // the caller's array is only read: the upstream class works on a copy (dataset.h:37-43)
     e = cudaMemcpyAsync(h->in_buf.ptr, data, in_bytes, cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) return fail(HPD_ERR_CUDA, cudaGetErrorString(e));
     rc = run(h, h->in_buf.ptr, n, d, dtype, static_cast<int64_t*>(h->out_buf.ptr), h->stream);
+    disarm_alloc_failure(h);
     if (rc) return rc;
     e = cudaMemcpyAsync(labels, h->out_buf.ptr, out_bytes, cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -191,6 +234,9 @@ int hpd_get_stats(const hpd_handle* h, hpd_stats* out) {
     out->extent_ms = h->last.index_ms[0];
     out->cells_sort_ms = h->last.index_ms[1];
     out->cell_table_ms = h->last.index_ms[2];
+    out->cell_ids_ms = h->last.cell_ids_ms;
+    out->rules_ms = h->last.rules_ms;
+    out->core_pairs = h->last.core_pairs;
     out->n_cells = h->last.n_cells;
     out->n_core = h->last.n_core;
     out->n_ambiguous = h->last.n_ambiguous;

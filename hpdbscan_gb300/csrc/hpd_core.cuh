@@ -17,8 +17,22 @@ __device__ __forceinline__ T shfl_val(T v, int src) {
 constexpr int kSparseQueries = 8;  // items with at most this many points use candidate lanes
 constexpr int kMaxRanges = 32;     // neighbour ranges kept in shared memory (3^d <= 32: d <= 3)
 
-template <typename T, int M, int D, bool PRUNE>
+// F: bit 0 (kCorePrune) selects the cells next to big dense cells, bit 1
+// (kCoreCount) counts the distance evaluations into a.pair_count (diagnostic pass).
+constexpr int kCorePrune = 1, kCoreCount = 2;
+
+template <typename T, int M, int D, int F>
 __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
+    constexpr bool PRUNE = (F & kCorePrune) != 0;
+    constexpr bool COUNT = (F & kCoreCount) != 0;
+    unsigned long long evals = 0;
+    auto flush_evals = [&]() {
+        if constexpr (COUNT) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
+            if (lane_id() == 0) atomicAdd(a.pair_count, evals);
+        }
+    };
     __shared__ int2 s_rng[4][kMaxRanges];
     const int w = threadIdx.x >> 5;
     const int item = blockIdx.x * 4 + w;
@@ -46,6 +60,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
         }
         if (__all_sync(0xffffffffu, !active || count >= limit)) {
             if (active) a.core[p] = 1;
+            flush_evals();
             return;
         }
     }
@@ -82,16 +97,19 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
                             c[k] = a.coords[(size_t)k * a.n + j];
                         }
                         hit = within_vals<T, M, D>(a, qq, c);
+                        if constexpr (COUNT) ++evals;
                     }
                     hits += __popc(__ballot_sync(0xffffffffu, hit));
                 }
             }
             if (lane_id() == 0) a.core[it.y + src] = hits >= limit ? 1 : 0;
         }
+        flush_evals();
         return;
     }
     auto aux_of = [](int) { return 0; };
     auto pair = [&](int, int u, int) {
+        if constexpr (COUNT) evals += active ? 1 : 0;
         if (active && within<T, M, D>(a, q, tile, u)) ++count;
     };
     auto done = [&]() { return __all_sync(0xffffffffu, !active || count >= limit); };
@@ -108,6 +126,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
                     return __any_sync(0xffffffffu, cls == kBoxEdge);
                 };
                 auto pair_edge = [&](int, int u, int) {
+                    if constexpr (COUNT) evals += (active && cur == kBoxEdge) ? 1 : 0;
                     if (cur == kBoxEdge && within<T, M, D>(a, q, tile, u)) ++count;
                 };
                 return !scan_dense<T, D>(a, tile, cr, q, active && count < limit, visit_group, aux_of, pair_edge,
@@ -117,6 +136,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
         return !scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
     });
     if (active) a.core[p] = count >= limit ? 1 : 0;
+    flush_evals();
 }
 
 }  // namespace hpd

@@ -30,6 +30,7 @@ struct Arena {
     size_t cap = 0;
     size_t used = 0;
     bool fixed = false;  // wraps memory it does not own: never allocates or frees
+    bool fail_next = false;  // test hook: the next reserve that must allocate fails instead
     cudaError_t reserve(size_t bytes);
     void reset() { used = 0; }
     // Hands out the next 256-byte aligned block; the caller reserves enough for all
@@ -45,9 +46,11 @@ struct Arena {
 };
 
 struct Timers {
-    cudaEvent_t ev[10] = {};
+    cudaEvent_t ev[12] = {};
     bool ok = false;
 };
+
+constexpr int kDefaultTiePassLimit = 1 << 20;  // far beyond any real input (tens of passes)
 
 struct Request {
     const void* d_data;  // row-major n x d of the element type, device memory
@@ -61,13 +64,17 @@ struct Request {
     int64_t* d_labels;   // device, input order
     cudaStream_t stream;
     bool no_dense = false;  // look cells up by binary search only (no grid-sized table)
+    int tie_pass_limit = kDefaultTiePassLimit;  // relaxation passes before HPD_ERR_TIMEOUT
+    bool count_pairs = false;  // diagnostic pass: count the core test's distance evaluations
 };
 
 struct RunInfo {
-    int64_t n_cells = 0, n_core = 0, n_ambiguous = 0, tie_iterations = 0;
+    int64_t n_cells = 0, n_core = 0, n_ambiguous = 0, tie_iterations = 0, core_pairs = 0;
     int launches = 0;
     float ms[7] = {0, 0, 0, 0, 0, 0, 0};  // total, index, core, union, border, tie-break, finalize
     float index_ms[3] = {0, 0, 0};          // extent, cell ids + sort, cell table
+    float cell_ids_ms = 0;                  // part of index_ms[1]: the cell id kernel
+    float rules_ms = 0;                     // part of ms[3]: resolving every core to its root
 };
 
 // Runs the whole pipeline for element type T.  Returns a Status and fills `err`.

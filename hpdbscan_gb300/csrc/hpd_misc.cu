@@ -16,6 +16,10 @@ __global__ void k_fill_int(int* p, int n, int v) {
 cudaError_t Arena::reserve(size_t bytes) {
     if (bytes <= cap) return cudaSuccess;
     if (fixed) return cudaErrorMemoryAllocation;
+    if (fail_next) {  // injected failure: nothing is freed or allocated
+        fail_next = false;
+        return cudaErrorMemoryAllocation;
+    }
     if (ptr) {
         cudaError_t e = cudaFree(ptr);
         ptr = nullptr;

@@ -221,7 +221,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     need += dense_k ? (size_t)dense_max * groups_cap * 2 * d * sizeof(T) : 0;   // sub-cell boxes
     need += dense_k ? (size_t)n * d * sizeof(T) : 0;                 // dense cells' coordinates by sub-cell
     need += (size_t)n * 4;                                           // second ambiguous list
-    need += (size_t)ncounts * 4 + (size_t)nscan * 8 + 64;
+    need += (size_t)ncounts * 4 + (size_t)nscan * 8 + 256;           // radix counts, scan scratch, totals, flags
     need += 64 * 256;                                                // alignment of up to 64 blocks
     HPD_CU(main.reserve(need));
     main.reset();
@@ -270,13 +270,14 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     uint32_t* counts = main.take<uint32_t>(ncounts);
     uint32_t* scan32 = main.take<uint32_t>(2 * nscan);
     uint32_t* totals = main.take<uint32_t>(4);   // cells, items, largest cell
-    int* flags_dev = main.take<int>(16);          // list counters, [6] cores, diagnostics, [13..15] range-check record
+    int* flags_dev = main.take<int>(32);          // list counters, [6] cores, [8..11] trace, [12] dense cells,
+                                                  // [13..15] range-check record, [16..17] pair count
     if (main.overflowed()) {
         err = "internal error: device buffer plan exceeds its reservation";
         return kRuntime;
     }
     int* guard = flags_dev + 13;
-    HPD_CU(cudaMemsetAsync(flags_dev, 0, 16 * sizeof(int), s));
+    HPD_CU(cudaMemsetAsync(flags_dev, 0, 32 * sizeof(int), s));
 
     // ---- cell ids (spatial_index.h:144-165)
     CellParams cp;
@@ -289,6 +290,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     const T* data = static_cast<const T*>(rq.d_data);
     k_cell_keys<T, K><<<blocks_for(n, 256), 256, 0, s>>>(data, n, cp, keys, vals);
     info.launches += 1;
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[9], s));
 
     // ---- stable sort by cell id (spatial_index.h:184-216)
     K* skeys = keys;
@@ -403,12 +405,16 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     } else if (rq.min_points > (uint64_t)n) {
         HPD_CU(cudaMemsetAsync(core, 0, n, s));
     } else {
-        if (prune) {
-            HPD_QUERY_DISPATCH_B(k_core, true, T, mode, d, qgrid, 128, qsmem, s, a);
-            info.launches += 1;
+        if (rq.count_pairs) {
+            // diagnostic pass: the same core test, counting its distance evaluations
+            a.pair_count = reinterpret_cast<unsigned long long*>(flags_dev + 16);
+            if (prune) HPD_QUERY_DISPATCH_B(k_core, kCorePrune | kCoreCount, T, mode, d, qgrid, 128, qsmem, s, a);
+            HPD_QUERY_DISPATCH_B(k_core, kCoreCount, T, mode, d, qgrid, 128, qsmem, s, a);
+        } else {
+            if (prune) HPD_QUERY_DISPATCH_B(k_core, kCorePrune, T, mode, d, qgrid, 128, qsmem, s, a);
+            HPD_QUERY_DISPATCH_B(k_core, 0, T, mode, d, qgrid, 128, qsmem, s, a);
         }
-        HPD_QUERY_DISPATCH_B(k_core, false, T, mode, d, qgrid, 128, qsmem, s, a);
-        info.launches += 1;
+        info.launches += prune ? 2 : 1;
     }
     if (timed) HPD_CU(cudaEventRecord(tm->ev[2], s));
 
@@ -426,6 +432,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     k_cell_uniform<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep, cell_flags);
     HPD_QUERY_DISPATCH(k_union_cells, T, mode, d, blocks_for(m, 4), 128, 0, s, a);
     HPD_QUERY_DISPATCH(k_union_cross, T, mode, d, qgrid, 128, qsmem, s, a);
+    if (timed) HPD_CU(cudaEventRecord(tm->ev[10], s));
     k_compress<<<blocks_for(n, 256), 256, 0, s>>>(parent, core, n, flags_dev + 6);
     info.launches += 8;
     if (timed) HPD_CU(cudaEventRecord(tm->ev[3], s));
@@ -477,7 +484,6 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         int* wls[2] = {wl0, wl1};
         int* wcounts[2] = {flags_dev + 3, flags_dev + 4};
         int cur = 0, wcur = 0;
-        const int kMaxTiePasses = 1 << 20;
         const int kPassesPerCheck = 4;
         const unsigned list_grid = 152 * 16;
         int h_left = h_amb;
@@ -521,7 +527,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         bool converged = false;
         while (h_left > 0 && !converged) {
             for (int k = 0; k < kPassesPerCheck; ++k) {
-                if (pass >= kMaxTiePasses) {
+                if (pass >= rq.tie_pass_limit) {
                     err = "border tie-break did not converge";
                     return kTimeout;
                 }
@@ -593,6 +599,12 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     HPD_CU(cudaMemcpyAsync(h_guard, guard, sizeof h_guard, cudaMemcpyDeviceToHost, s));
     HPD_CU(cudaGetLastError());
     HPD_CU(cudaStreamSynchronize(s));
+    if (rq.count_pairs) {
+        unsigned long long pairs = 0;
+        HPD_CU(cudaMemcpyAsync(&pairs, flags_dev + 16, sizeof pairs, cudaMemcpyDeviceToHost, s));
+        HPD_CU(cudaStreamSynchronize(s));
+        info.core_pairs = (int64_t)pairs;
+    }
     if (h_guard[0]) {
         err = "internal error: device index out of range (check " + std::to_string(h_guard[1]) + ", index " +
               std::to_string(h_guard[2]) + ", " + std::to_string(h_guard[0]) + " times)";
@@ -608,6 +620,8 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         cudaEventElapsedTime(&ms, tm->ev[0], tm->ev[7]); info.index_ms[0] = ms;
         cudaEventElapsedTime(&ms, tm->ev[7], tm->ev[8]); info.index_ms[1] = ms;
         cudaEventElapsedTime(&ms, tm->ev[8], tm->ev[1]); info.index_ms[2] = ms;
+        cudaEventElapsedTime(&ms, tm->ev[7], tm->ev[9]); info.cell_ids_ms = ms;
+        cudaEventElapsedTime(&ms, tm->ev[10], tm->ev[3]); info.rules_ms = ms;
     }
     return kOk;
 }

@@ -205,6 +205,7 @@ struct QueryArgs {
     const T* dense_coords;  // [d][n] coordinates of dense cells' points in dense_sec order
     int* amb_out;         // undecided ambiguous borders after a decision round
     int* n_amb_out;
+    unsigned long long* pair_count;  // diagnostic pass: distance evaluations of the core test
 };
 
 // Per-warp tile in shared memory: d planes of 32 coordinates plus one aux word.

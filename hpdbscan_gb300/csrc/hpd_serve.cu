@@ -112,6 +112,7 @@ int run_job(WorkerState& ws, hpd_job& j) {
 
 int validate(const hpd_job* j) {
     if (!j) return fail(HPD_ERR_INVALID, "null job");
+    if (!(j->deadline_ms >= 0)) return fail(HPD_ERR_INVALID, "deadline must be >= 0");
     if (!(j->epsilon > 0.0f)) return fail(HPD_ERR_INVALID, "epsilon needs to be positive");
     if (elem_size(j->dtype) == 0) return fail(HPD_ERR_UNSUPPORTED, "element type not supported by this build");
     if (j->n < 0 || j->n > INT32_MAX - 1 || j->d < 1) return fail(HPD_ERR_INVALID, "bad shape");
@@ -144,31 +145,37 @@ void hpd_server::worker(WorkerState* ws, int64_t reserve_points, int reserve_dim
     for (;;) {
         int64_t ticket = 0;
         hpd_job* job = nullptr;
+        bool late = false;
         {
             std::unique_lock<std::mutex> lock(mu);
-            cv_work.wait(lock, [&] {
+            // a job past its deadline leaves the queue at once, without budget
+            auto expired = [&](const Entry& en) {
+                return en.job->deadline_ms > 0 && ms_between(en.submit, Clock::now()) > en.job->deadline_ms;
+            };
+            cv_work.wait_for(lock, std::chrono::milliseconds(5), [&] {
                 if (stop) return true;
                 if (queue.empty()) return false;
                 const Entry& head = entries[queue.front()];
-                return in_flight == 0 || in_flight + head.bytes <= budget;
+                return in_flight == 0 || in_flight + head.bytes <= budget || expired(head);
             });
             if (stop && queue.empty()) break;
             if (queue.empty()) continue;
             ticket = queue.front();
             Entry& en = entries[ticket];
-            if (!(in_flight == 0 || in_flight + en.bytes <= budget)) continue;
+            late = expired(en);
+            if (!late && !(in_flight == 0 || in_flight + en.bytes <= budget)) continue;
             queue.pop_front();
-            in_flight += en.bytes;
+            if (!late) in_flight += en.bytes;
             en.start = Clock::now();
             job = en.job;
         }
-        const int rc = job->n > 0 ? run_job(*ws, *job) : HPD_OK;
+        const int rc = late ? HPD_ERR_TIMEOUT : (job->n > 0 ? run_job(*ws, *job) : HPD_OK);
         {
             std::lock_guard<std::mutex> lock(mu);
             Entry& en = entries[ticket];
             en.end = Clock::now();
             en.done = true;
-            in_flight -= en.bytes;
+            if (!late) in_flight -= en.bytes;
             job->status = rc;
             job->queue_ms = ms_between(en.submit, en.start);
             job->run_ms = ms_between(en.start, en.end);

@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(128) k_tie_greedy(QueryArgs<T> a) {
     if (active) {
         // positions below the component's threshold are settled already (value p)
         const int root = a.parent[p];
-        active = p <= a.tmax[root] && p >= a.tlow[root];
+        active = in_range(a.guard, root, a.n, kGuardRoot) && p <= a.tmax[root] && p >= a.tlow[root];
     }
     if (!__any_sync(0xffffffffu, active)) return;
     const Tile<T> tile = warp_tile<T>(a.g.d);
@@ -426,8 +426,15 @@ __global__ void __launch_bounds__(128) k_tie_decide(QueryArgs<T> a, int final_pa
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) other = min(other, __shfl_xor_sync(0xffffffffu, other, o));
     if (lane_id() == 0) {
-        if (final_pass || ub < other) a.broot[b] = root_best;
-        else a.amb_out[atomicAdd(a.n_amb_out, 1)] = b;
+        if (best == ~0ull) {
+            // an ambiguous border has core neighbours of two components by construction
+            in_range(a.guard, -1, a.n, kGuardAmbiguous);
+        } else if (final_pass || ub < other) {
+            a.broot[b] = root_best;
+        } else {
+            const int k = atomicAdd(a.n_amb_out, 1);
+            if (in_range(a.guard, k, a.n, kGuardList)) a.amb_out[k] = b;
+        }
     }
 }
 

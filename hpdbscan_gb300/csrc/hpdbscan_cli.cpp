@@ -221,13 +221,21 @@ int main(int argc, char** argv) {
         hpd_stats st;
         hpd_get_stats(h, &st);
         auto s = [](double ms) { return ms / 1000.0; };
+        // the upstream phases (hpdbscan.h:376-458, spatial_index.h:549-602) from the engine's:
+        //   dimensions  per-dimension extent, grid and dimension order
+        //   cells       cell id of every point + cell table (upstream: ids + histogram index)
+        //   sorting     stable radix sort by cell id + gather of the coordinates
+        //   DBSCAN      core test, connectivity, borders and their tie-break
+        //   rules       every core resolved to its cluster root (upstream: apply_rules)
+        //   order       labels scattered back to input order
         std::cout << "Computing cell space" << std::endl
                   << "\tComputing dimensions...[OK] in " << s(st.extent_ms) << std::endl
-                  << "\tComputing cells...     [OK] in " << s(st.cells_sort_ms) << std::endl
-                  << "\tSorting points...      [OK] in " << s(st.cell_table_ms) << std::endl
+                  << "\tComputing cells...     [OK] in " << s(st.cell_ids_ms + st.cell_table_ms) << std::endl
+                  << "\tSorting points...      [OK] in " << s(st.cells_sort_ms - st.cell_ids_ms) << std::endl
                   << "Clustering..." << std::endl
-                  << "\tDBSCAN...              [OK] in " << s(st.core_ms + st.union_ms + st.border_ms) << std::endl
-                  << "\tAppyling rules...      [OK] in " << s(st.tie_ms) << std::endl
+                  << "\tDBSCAN...              [OK] in "
+                  << s(st.core_ms + st.union_ms - st.rules_ms + st.border_ms + st.tie_ms) << std::endl
+                  << "\tAppyling rules...      [OK] in " << s(st.rules_ms) << std::endl
                   << "\tRecovering order...    [OK] in " << s(st.finalize_ms) << std::endl;
         std::set<int64_t> unique;
         size_t cluster_points = 0, noise_points = 0, core_points = 0;

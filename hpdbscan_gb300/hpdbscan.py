@@ -14,6 +14,7 @@ array.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -57,10 +58,27 @@ class HPDBSCAN:
         neighbours (faster; cores, noise and other borders unchanged)."""
         _lib.raise_for(self._lib.hpd_set_tie_break(self._h, mode))
 
+    def set_tie_pass_limit(self, passes: int = 0) -> None:
+        """Relaxation passes of the exact tie-break before HPD_ERR_TIMEOUT; 0: default."""
+        _lib.raise_for(self._lib.hpd_set_tie_pass_limit(self._h, int(passes)))
+
+    def set_diagnostics(self, flags: int = 0) -> None:
+        """DIAG_COUNT_PAIRS: count the core test's distance evaluations (stats core_pairs)."""
+        _lib.raise_for(self._lib.hpd_set_diagnostics(self._h, int(flags)))
+
+    def debug_inject(self, what: int) -> None:
+        """Test hook for the next call: INJECT_FAIL_ALLOC."""
+        _lib.raise_for(self._lib.hpd_debug_inject(self._h, int(what)))
+
     def cluster(self, data, dataset: str | None = None, threads: int | None = None):
         """cluster(ndarray) | cluster(path, dataset[, threads]) -> tuple of int."""
         if isinstance(data, (str, bytes)):
-            raise ValueError("Could not open " + (data if isinstance(data, str) else data.decode()))
+            path = data if isinstance(data, str) else data.decode()
+            # as the C++ header's file overload: a missing file is std::invalid_argument
+            # ("Could not open"), an existing one std::runtime_error (no HDF5 reader here)
+            if not os.path.isfile(path):
+                raise ValueError("Could not open " + path)
+            raise RuntimeError("HDF5 input is not supported by this build")
         arr = np.ascontiguousarray(np.asarray(data, dtype=np.float64))
         return tuple(self.cluster_array(arr).tolist())
 

@@ -21,7 +21,7 @@ from . import _lib
 _CODES = {np.dtype(np.float32): _lib.F32, np.dtype(np.float64): _lib.F64}
 
 
-def _job(points, eps, min_points):
+def _job(points, eps, min_points, deadline_ms=0.0):
     pts = np.ascontiguousarray(points)
     if pts.ndim != 2 or pts.dtype not in _CODES:
         raise ValueError("jobs take (n, d) float32 or float64 arrays")
@@ -33,6 +33,7 @@ def _job(points, eps, min_points):
     j.epsilon = float(eps)
     j.min_points = int(min_points)
     j.labels = labels.ctypes.data
+    j.deadline_ms = float(deadline_ms)
     return j, pts, labels
 
 
@@ -66,8 +67,10 @@ class Server:
         self._h = h
         self._pending = {}
 
-    def submit(self, points, eps, min_points) -> int:
-        job = _job(points, eps, min_points)
+    def submit(self, points, eps, min_points, deadline_ms: float = 0.0) -> int:
+        """Queue a job; one still waiting for a worker deadline_ms after submission fails
+        with HPD_ERR_TIMEOUT (TimeoutError from wait) without running."""
+        job = _job(points, eps, min_points, deadline_ms)
         t = ctypes.c_int64()
         rc = self._lib.hpd_server_submit(self._h, ctypes.byref(job[0]), ctypes.byref(t))
         if rc:
@@ -83,6 +86,8 @@ class Server:
     def wait(self, ticket: int, with_stats: bool = False):
         job = self._pending.pop(ticket)
         status = self._lib.hpd_server_wait(self._h, ticket)
+        if status == _lib.HPD_ERR_TIMEOUT:
+            raise TimeoutError("job passed its deadline before a worker took it")
         if status:
             raise RuntimeError(f"job failed with status {status}")
         if with_stats:

@@ -79,6 +79,9 @@ typedef struct {
     double extent_ms;      /* part of index_ms: per-dimension min / max */
     double cells_sort_ms;  /* part of index_ms: cell ids, radix sort, gather */
     double cell_table_ms;  /* part of index_ms: cell table and work items */
+    double cell_ids_ms;    /* part of cells_sort_ms: the cell id of every point */
+    double rules_ms;       /* part of union_ms: every core resolved to its cluster root */
+    int64_t core_pairs;    /* distance evaluations of the core test (HPD_DIAG_COUNT_PAIRS only) */
 } hpd_stats;
 
 /* HPDBSCAN(epsilon, min_points): fails with HPD_ERR_INVALID and the upstream
@@ -97,6 +100,24 @@ int hpd_set_arith(hpd_handle* h, int cell_mode, int dist_mode);
  * border keep their exact labels.  No counterpart in the reference. */
 typedef enum { HPD_TIE_EXACT = 0, HPD_TIE_SMALLEST_ID = 1 } hpd_tie_mode;
 int hpd_set_tie_break(hpd_handle* h, int mode);
+
+/* Bound of the exact tie-break (no counterpart in the reference): it relaxes the
+ * reference's provisional labels pass by pass until no value changes; a call that
+ * would need more than `passes` passes gives up with HPD_ERR_TIMEOUT and the handle
+ * stays usable.  0 restores the default (2^20 passes). */
+int hpd_set_tie_pass_limit(hpd_handle* h, int32_t passes);
+
+/* Diagnostics (no counterpart in the reference).  HPD_DIAG_COUNT_PAIRS: the core test
+ * counts the distance evaluations it performs into hpd_stats.core_pairs (slower; for
+ * measurement runs only).  0 turns diagnostics off. */
+typedef enum { HPD_DIAG_COUNT_PAIRS = 1 } hpd_diag;
+int hpd_set_diagnostics(hpd_handle* h, int32_t flags);
+
+/* Test hook (no counterpart in the reference) for the next call on the handle:
+ * HPD_INJECT_FAIL_ALLOC makes the first device allocation the call needs fail without
+ * being attempted, so the call returns HPD_ERR_NOMEM. */
+typedef enum { HPD_INJECT_FAIL_ALLOC = 1 } hpd_inject;
+int hpd_debug_inject(hpd_handle* h, int32_t what);
 
 /* Labels for n points of d coordinates (row-major, host memory) into labels[n]
  * (host memory), in input order.  `threads` is accepted for interface parity and
@@ -129,6 +150,9 @@ typedef struct {
     int32_t status;        /* out: hpd_status of the job, -1 while pending */
     double queue_ms;       /* out: submission to start */
     double run_ms;         /* out: start to labels on the host */
+    double deadline_ms;    /* in: a job still waiting for a worker this long after its
+                            * submission completes with HPD_ERR_TIMEOUT without running;
+                            * 0 = no deadline */
 } hpd_job;
 
 /* Runs every job of the array on the current GPU with n_workers concurrent streams
