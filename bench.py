@@ -10,17 +10,24 @@ One step = one full clustering (grid index, core test, connectivity, borders and
 tie-break, labels in input order).  `value` times steps on device-resident input
 with CUDA events on the engine's stream, flushing L2 (256 MiB write) between steps;
 `e2e` times the host-buffer C-ABI call (pinned input copied in, int64 labels copied
-out) on the same workload.  With --gpus N > 1 (torchrun) every rank clusters its own
-replica of the workload (no data-path collective; the path does not shard) and the
-job value is N x points / the slowest rank's time.
+out) on the same workload.  After the timed region the labels are hashed and compared
+with the upstream single-thread build's (tests/golden/fullsize/blobs10m_s0.npz).
+With --gpus N > 1 (torchrun) every rank clusters its own replica of the workload (no
+data-path collective; the path does not shard) and the job value is
+N x points / the slowest rank's time.
+
+`roofline` is the core test's; `roofline_phases` gives every phase against the bytes
+(and, for the core test, the flops and distance evaluations) it must move.
 
 `skewed` times the 50M-point skewed 2-D density workload (cells of up to 2.2M points) the
 same way as `value`.
 
---impl reference times the CPU implementation of the same path on the host cores:
-the upstream build when it exists on this host, else the C restatement run with the
-upstream's parallel structure (OpenMP, all host threads), on a spatial crop of the
-workload that keeps its density.
+--impl reference times the upstream build (the reference's own headers compiled with
+its own flags on this host: oracle/_ref) with all host threads: each step clusters a
+spatial slab of the workload that keeps its density; the line also carries one run on
+the whole 10M-point workload and a single-thread run on a smaller slab.  Without the
+upstream build it falls back to the C restatement run with the upstream's parallel
+structure.
 """
 from __future__ import annotations
 
@@ -40,7 +47,25 @@ sys.path.insert(0, ROOT)
 METRIC = "Mpoints/s clustered (10M 3-D, bit-exact labels)"
 WORKLOAD = "blobs_10m: 10,000,000 x 3 float32, 200 blobs + 5% noise, eps=0.005, minPoints=16, seed 0"
 PROFILE = os.path.join(ROOT, "profiles", "k_core_blobs10m.txt")
+FIXTURE = os.path.join(ROOT, "tests", "golden", "fullsize", "blobs10m_s0.npz")
 CROP = 0.10  # CPU sample: spatial crop of the workload (keeps its density)
+CROP_1T = 0.02  # single-thread CPU sample
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal non-tensor FP32 (FMA = 2 flops) at 2.07 GHz
+
+
+def workload_config(n, d, eps, min_points, world):
+    """The `config` of both arms (engine and reference), so that they name one workload."""
+    return {"workload": WORKLOAD, "n_points": n, "dims": d, "eps": eps, "min_points": min_points,
+            "parallelism": "replicas" if world > 1 else "single", "l2": "flushed between steps (256 MiB write)"}
+
+
+def labels_match_upstream(labels):
+    """sha256 of the int64 labels against the upstream single-thread build's (None: no fixture)."""
+    import hashlib
+    if not os.path.exists(FIXTURE):
+        return None
+    z = np.load(FIXTURE)
+    return hashlib.sha256(np.ascontiguousarray(labels, dtype=np.int64).tobytes()).hexdigest() == str(z["labels_sha256"])
 
 
 T0 = time.perf_counter()
@@ -176,9 +201,9 @@ def cpu_sample(points, eps, min_points, frac):
     return np.ascontiguousarray(sel)
 
 
-def time_cpu(points, eps, min_points, steps):
+def time_cpu(points, eps, min_points, steps, threads=None):
     from oracle import pyoracle
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     if pyoracle.ref_available():
         kind, fn = "reference", lambda: pyoracle.ref_cluster(points, eps, min_points, threads=threads)
     else:
@@ -299,16 +324,32 @@ def run_reference(args):
     from oracle import pyoracle
     pyoracle.build(ref=None)
     w = workloads.blobs_10m(seed=0)
+    n, d = w.points.shape
     crop = cpu_sample(w.points, w.eps, w.min_points, CROP)
+    progress(f"reference steps on a {len(crop)}-point slab")
     kind, threads, ts = time_cpu(crop, w.eps, w.min_points, args.warmup + args.steps)
     timed = ts[args.warmup:]
     val = len(crop) * len(timed) / sum(timed) / 1e6
-    sample = f"slab of {len(crop)} points around the median x of the 10M workload ({CROP:.0%}), same eps/minPoints"
+    sample = (f"each step: the slab of {len(crop)} points around the median x of the 10M workload "
+              f"({CROP:.0%}, same density, eps and minPoints), {threads} threads")
+    full = None
+    if args.reference_full:
+        progress("reference on the whole workload")
+        _, _, tf = time_cpu(w.points, w.eps, w.min_points, 1)
+        full = {"points": n, "seconds": tf[0], "value": n / tf[0] / 1e6, "threads": threads,
+                "note": "one run on the whole 10M-point workload"}
+    progress("reference, one thread")
+    crop1 = cpu_sample(w.points, w.eps, w.min_points, CROP_1T)
+    _, _, t1 = time_cpu(crop1, w.eps, w.min_points, 1, threads=1)
+    one = {"points": len(crop1), "seconds": t1[0], "value": len(crop1) / t1[0] / 1e6, "threads": 1,
+           "note": f"slab of {len(crop1)} points around the median x ({CROP_1T:.0%})"}
+    import platform
     line = {"metric": METRIC, "value": val, "unit": "Mpoints/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * sum(timed) / len(timed), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": sample}, "impl": "reference",
-            "cpu_baseline": {"value": val, "unit": "Mpoints/s", "cores": threads, "kind": kind, "sample": sample},
+            "config": workload_config(n, d, w.eps, w.min_points, world), "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": "Mpoints/s", "cores": threads, "kind": kind, "sample": sample,
+                             "host": platform.machine(), "full_workload": full, "single_thread": one},
             "e2e": {"value": val, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -395,9 +436,17 @@ def run_engine(args):
     e2e_total = slowest_rank(sum(e2e_s), world, "cuda")
     e2e_value = job_mpoints_per_s(n, args.steps, world, e2e_total)
     same = bool(torch.equal(host_labels.cuda(), labels))
+    exact = labels_match_upstream(labels.cpu().numpy())
 
     if rank != 0:
         return
+    # untimed diagnostic pass: the core test's distance evaluations
+    from hpdbscan_gb300 import _lib as L
+    hd = HPDBSCAN(w.eps, w.min_points)
+    hd.set_diagnostics(L.DIAG_COUNT_PAIRS)
+    hd.cluster_device(x.data_ptr(), n, d, np.float32, labels.data_ptr(), stream.cuda_stream)
+    core_pairs = int(hd.stats()["core_pairs"])
+    del hd
     peak, peak_kind = load_peaks()
     core_bytes, cand = candidate_bytes(w.points, w.eps)
     core_avg = sum(core_ms) / len(core_ms)
@@ -416,13 +465,36 @@ def run_engine(args):
     progress("skewed density")
     skewed = measure_skewed(args.skewed_points) if args.skewed_points > 0 else None
     progress("done")
+    ph = {k: mean(k + "_ms") for k in ("index", "core", "union", "border", "tie", "finalize")}
+    n_cells = int(phases[-1]["n_cells"])
+    b_index = n * (4 * d + 4 * d + 4 + 4) + 8 * n_cells  # coordinates in and sorted out, index and key, cell table
+    b_graph = n * (8 + 4) * 2  # label + parent, read and written once: the minimum of any union / label pass
+
+    def frac(b, ms):
+        a = b / (ms / 1000) / 1e9
+        return {"achieved_gbs": round(a, 1), "frac": round(a / peak, 4), "bytes": b, "ms": round(ms, 4)}
+    core_flops = core_pairs * 3 * d
+    roof_phases = {
+        "index": {"bound": "hbm", **frac(b_index, ph["index"])},
+        "core": {"bound": "issue (fp32)", **frac(core_bytes, ph["core"]),
+                 "distance_evals": core_pairs, "distance_evals_per_s": core_pairs / (ph["core"] / 1000),
+                 "fp32_tflops": core_flops / (ph["core"] / 1000) / 1e12,
+                 "fp32_frac": core_flops / (ph["core"] / 1000) / 1e12 / FP32_PEAK_TFLOPS,
+                 "fp32_peak_tflops": round(FP32_PEAK_TFLOPS, 1),
+                 "fp32_peak_source": "nominal: 152 SMs x 128 lanes x 2 (FMA) x 2.07 GHz",
+                 "reference_equivalent_evals_per_s": cand / (ph["core"] / 1000)},
+        "union": {"bound": "latency (union-find)", **frac(b_graph, ph["union"])},
+        "border": {"bound": "latency", **frac(b_graph, ph["border"])},
+        "tie": {"bound": "latency (relaxation passes)", **frac(b_graph, ph["tie"])},
+        "finalize": {"bound": "hbm", **frac(n * (1 + 4 + 4 + 4 + 8), ph["finalize"])},
+    }
     line = {
         "metric": METRIC, "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_points": n, "dims": d, "eps": w.eps, "min_points": w.min_points,
-                   "parallelism": "replicas" if world > 1 else "single", "l2": "flushed between steps (256 MiB write)",
-                   "labels_match_e2e": same},
+        "config": workload_config(n, d, w.eps, w.min_points, world),
+        "labels_match_e2e": same,
+        "labels_bit_exact_vs_upstream": exact,
         "e2e": {"value": e2e_value, "unit": "Mpoints/s", "h2d_bytes_per_step": n * d * 4, "d2h_bytes_per_step": n * 8,
                 "ms_per_step": 1000 * e2e_total / args.steps},
         "roofline": {"bound": "hbm", "kernel": "k_core (neighbour count, early exit at minPoints)",
@@ -430,7 +502,8 @@ def run_engine(args):
                      "peak_source": f"{peak_kind} hbm_gbs",
                      "traffic": profile_traffic(), "algorithmic_bytes": core_bytes, "candidate_pairs": cand,
                      "avg_launch_ms": core_avg},
-        "phases_ms": {k: round(mean(k + "_ms"), 4) for k in ("index", "core", "union", "border", "tie", "finalize")},
+        "roofline_phases": roof_phases,
+        "phases_ms": {k: round(v, 4) for k, v in ph.items()},
         "cpu_baseline": {"value": cpu_val, "unit": "Mpoints/s", "cores": threads, "kind": kind,
                          "sample": f"slab of {len(crop)} points around the median x of the 10M workload "
                                    f"({CROP:.0%}), median of 2 runs"},
@@ -455,6 +528,8 @@ def main():
     ap.add_argument("--batch-instances", type=int, default=256, help="batch workload instances (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="length of the serving trace (0: skip)")
     ap.add_argument("--skewed-points", type=int, default=50_000_000, help="skewed 2-D workload size (0: skip)")
+    ap.add_argument("--reference-full", type=int, default=1,
+                    help="reference arm: also cluster the whole 10M workload once (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
