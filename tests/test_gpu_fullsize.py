@@ -1,68 +1,72 @@
-"""Full-size checks on the 10M-point benchmark workload (size-independent properties).
+"""Full-size workloads against the upstream single-thread build, bit for bit.
 
-The single-thread oracle is too slow for 10M points in a test, so the GPU labels are
-checked against the oracle run with the upstream's own parallel structure (all host
-threads), whose core/noise flags and core labels are deterministic, and against
-properties that hold for every correct labelling:
+The upstream HPDBSCAN::cluster<float>(data, n, d, threads=1) takes minutes on these
+inputs, so its labels are pinned by tests/golden/make_fullsize.py into
+tests/golden/fullsize/<set>.npz: the sha256 of the input the generator makes, the
+sha256 of the full int64 label vector, the core / border / noise counts and, for
+diagnostics, every border point with cores of several clusters within eps together
+with its upstream label.  A test here regenerates the input, clusters it on the GPU
+and requires the identical label vector (same sha256); on a mismatch it reports which
+kind of point differs.
 
-* core / noise flags and every core label identical to the oracle's;
-* cluster k's first core: the point at cell-sorted position k - 1 is a core labelled -k;
-* every border label k names a cluster with a core point within eps of the border;
-* borders differ from the multi-threaded oracle only where that oracle itself is
-  free to differ (borders next to several clusters), i.e. on a tiny fraction;
-* two runs give identical labels.
+Sets: the 10M-point 3-D benchmark workload (eps 0.005, minPoints 16) and the skewed
+2-D density at 1M points (eps 1e-3, minPoints 32).
 """
+import hashlib
 import os
 
 import numpy as np
 import pytest
 
+from conftest import GOLDEN
+
 pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+FULL = os.path.join(GOLDEN, "fullsize")
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _load(name, make):
+    z = np.load(os.path.join(FULL, name + ".npz"))
+    w = make()
+    assert _sha(w.points) == str(z["points_sha256"]), "regenerated points differ from the fixture's (numpy version?)"
+    return w, z
+
+
+def _check(got, z):
+    if _sha(got.astype(np.int64)) == str(z["labels_sha256"]):
+        return
+    amb, want = z["amb_index"], z["amb_label"]
+    detail = (f"core {(got < 0).sum()} vs {int(z['n_core'])}, border {(got > 0).sum()} vs {int(z['n_border'])}, "
+              f"noise {(got == 0).sum()} vs {int(z['n_noise'])}; "
+              f"multi-cluster borders differing {(got[amb] != want).sum()} of {len(amb)}")
+    pytest.fail("labels differ from the upstream single-thread build: " + detail)
 
 
 @pytest.fixture(scope="module")
-def full(gpu, oracle):
+def blobs10m(gpu):
     from hpdbscan_gb300 import HPDBSCAN, workloads
-    w = workloads.blobs_10m(seed=0)
+    w, z = _load("blobs10m_s0", lambda: workloads.blobs_10m(seed=0))
     h = HPDBSCAN(w.eps, w.min_points)
     got = h.cluster_array(w.points)
     again = h.cluster_array(w.points)
-    threads = os.cpu_count() or 1
-    want, order, _ = oracle.cluster(w.points, w.eps, w.min_points, threads=threads, with_order=True)
-    return w, got, again, want, order, h.stats()
+    return w, z, got, again
 
 
-def test_repeatable(full):
-    _, got, again, *_ = full
+def test_blobs10m_bit_exact(blobs10m):
+    _, z, got, _ = blobs10m
+    _check(got, z)
+
+
+def test_blobs10m_repeatable(blobs10m):
+    _, _, got, again = blobs10m
     assert np.array_equal(got, again)
 
 
-def test_core_and_noise_identical(full):
-    _, got, _, want, _, _ = full
-    assert np.array_equal(got < 0, want < 0)
-    assert np.array_equal(got == 0, want == 0)
-    core = want < 0
-    assert np.array_equal(got[core], want[core])
-
-
-def test_cluster_ids_are_first_core_positions(full):
-    _, got, _, _, order, _ = full
-    ids = np.unique(np.abs(got[got != 0]))
-    first = order[ids - 1]  # input index of the point at sorted position k - 1
-    assert np.array_equal(got[first], -ids)
-
-
-def test_borders_attach_to_adjacent_clusters(full):
-    ckdtree = pytest.importorskip("scipy.spatial").cKDTree
-    w, got, _, want, _, stats = full
-    border = np.flatnonzero(got > 0)
-    core = np.flatnonzero(got < 0)
-    tree = ckdtree(w.points[core].astype(np.float64))
-    # every border whose label differs from the parallel oracle, and a sample of the rest
-    differ = border[got[border] != want[border]]
-    rng = np.random.default_rng(0)
-    sample = np.concatenate([differ, rng.choice(border, size=min(20000, len(border)), replace=False)])
-    hits = tree.query_ball_point(w.points[sample].astype(np.float64), r=w.eps * (1 + 1e-5))
-    for b, nb in zip(sample, hits):
-        assert np.any(got[core[nb]] == -got[b]), int(b)
-    assert len(differ) <= max(10, stats["n_ambiguous"])
+def test_skewed1m_bit_exact(gpu):
+    from hpdbscan_gb300 import HPDBSCAN, workloads
+    w, z = _load("skewed1m_s0", lambda: workloads.skewed_2d(seed=0, n=1_000_000))
+    _check(HPDBSCAN(w.eps, w.min_points).cluster_array(w.points), z)
