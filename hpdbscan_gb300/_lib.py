@@ -15,7 +15,7 @@ HPD_ERR_GRID, HPD_ERR_NOMEM, HPD_ERR_CUDA, HPD_ERR_TIMEOUT = 4, 5, 6, 7
 
 F32, F64, I8, I16, I32, I64, U8, U16, U32, U64 = range(10)
 CELL_RECIP, CELL_DIV = 0, 1
-DIST_GCC_X86, DIST_SEQ, DIST_SEQ_FMA = 0, 1, 2
+DIST_GCC_X86, DIST_SEQ, DIST_SEQ_FMA, DIST_GCC_AARCH64 = 0, 1, 2, 3
 TIE_EXACT, TIE_SMALLEST_ID = 0, 1
 DIAG_COUNT_PAIRS = 1
 INJECT_FAIL_ALLOC = 1

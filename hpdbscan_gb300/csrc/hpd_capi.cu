@@ -142,7 +142,7 @@ void hpd_destroy(hpd_handle* h) {
 int hpd_set_arith(hpd_handle* h, int cell_mode, int dist_mode) {
     if (!h) return fail(HPD_ERR_INVALID, "null handle");
     if (cell_mode != HPD_CELL_RECIP && cell_mode != HPD_CELL_DIV) return fail(HPD_ERR_INVALID, "bad cell mode");
-    if (dist_mode < HPD_DIST_GCC_X86 || dist_mode > HPD_DIST_SEQ_FMA) return fail(HPD_ERR_INVALID, "bad distance mode");
+    if (dist_mode < HPD_DIST_GCC_X86 || dist_mode > HPD_DIST_GCC_AARCH64) return fail(HPD_ERR_INVALID, "bad distance mode");
     h->cell_mode = cell_mode;
     h->dist_mode = dist_mode;
     return HPD_OK;

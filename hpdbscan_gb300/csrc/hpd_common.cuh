@@ -40,7 +40,12 @@ struct Grid {
 // Summation orders of sum_k (p_k - q_k)^2, each reproducing one compilation of the
 // reference's loop (spatial_index.h:751-754) exactly.  All operations are
 // explicitly rounded intrinsics, so nvcc never contracts or reassociates them.
-enum DistMode : int { kDistGccX86 = HPD_DIST_GCC_X86, kDistSeq = HPD_DIST_SEQ, kDistSeqFma = HPD_DIST_SEQ_FMA };
+enum DistMode : int {
+    kDistGccX86 = HPD_DIST_GCC_X86,
+    kDistSeq = HPD_DIST_SEQ,
+    kDistSeqFma = HPD_DIST_SEQ_FMA,
+    kDistGccArm = HPD_DIST_GCC_AARCH64
+};
 
 __device__ __forceinline__ float sq_(float t) { return __fmul_rn(t, t); }
 __device__ __forceinline__ double sq_(double t) { return __dmul_rn(t, t); }
@@ -57,7 +62,41 @@ __device__ __forceinline__ double fma_(double a, double b, double c) { return __
 template <typename F, int M, int D>
 __device__ __forceinline__ F fold_sq(const F* t, int d) {
     const int n = D > 0 ? D : d;
-    if (M == kDistSeq || (M == kDistGccX86 && n <= 3)) {
+    if (M == kDistGccArm) {
+        // GCC -Ofast on aarch64 (NEON): float from 4 dimensions and double from 2 on,
+        // lanes (4 / 2) accumulate dimensions k = j (mod lanes) with fused
+        // multiply-adds, are folded pairwise ((l0 + l1) + (l2 + l3), or l0 + l1), and
+        // the remaining dimensions are added with fused multiply-adds; below that, a
+        // fused running sum.
+        constexpr int L = sizeof(F) == 4 ? 4 : 2;
+        const int nv = n >= L ? (n & ~(L - 1)) : 0;
+        F s = 0;
+        int j = 0;
+        if (nv) {
+            F l[L];
+#pragma unroll
+            for (int k = 0; k < L; ++k) l[k] = sq_(t[k]);
+#pragma unroll
+            for (int jj = L; jj < (D > 0 ? D : kMaxDims); jj += L) {
+                if (jj + L - 1 >= (D > 0 ? D : kMaxDims) || jj >= nv) break;
+#pragma unroll
+                for (int k = 0; k < L; ++k) l[k] = fma_(t[jj + k], t[jj + k], l[k]);
+            }
+            if constexpr (L == 4) s = add_(add_(l[0], l[1]), add_(l[2], l[3]));
+            else s = add_(l[0], l[1]);
+            j = nv;
+        } else {
+            s = sq_(t[0]);
+            j = 1;
+        }
+#pragma unroll
+        for (int k = 1; k < (D > 0 ? D : kMaxDims); ++k) {
+            if (k < j) continue;
+            if (k >= n) break;
+            s = fma_(t[k], t[k], s);
+        }
+        return s;
+    } else if (M == kDistSeq || (M == kDistGccX86 && n <= 3)) {
         F off = sq_(t[0]);
 #pragma unroll
         for (int k = 1; k < (D > 0 ? D : kMaxDims); ++k) {

@@ -67,15 +67,61 @@ __host__ __device__ __forceinline__ typename Elem<T>::F diff_f(T x, T mn) {
     else return (float)(T)(x - mn);
 }
 
-// EPS2 = (T)(float)(eps * eps) (hpdbscan.h:53 then the region query's T parameter),
-// with the conversions GCC emits for the narrow integer types.
+// EPS2 = (T)(float)(eps * eps) (hpdbscan.h:53, then the region query's T parameter)
+// as GCC compiles the float -> integer conversion for the reference's target.  The
+// conversions are spelled out, so that the result does not depend on the compiler
+// of this library.  x86-64 (cvttss2si): a 32-bit result for types below 32 bits and
+// for int32, a 64-bit result for uint32 and int64, GCC's two-step sequence around
+// 2^63 for uint64; out of range gives the "integer indefinite" 0x80...0.  aarch64
+// (fcvtzs / fcvtzu into a 32-bit register up to 32 bits, a 64-bit one above): saturate.
+struct Eps2Conv {
+    static int64_t x86_32(float f) {
+        return (f > -2147483649.0f && f < 2147483648.0f) ? (int64_t)(int32_t)f : (int64_t)INT32_MIN;
+    }
+    static int64_t x86_64(float f) {
+        return (f >= -9223372036854775808.0f && f < 9223372036854775808.0f) ? (int64_t)f : INT64_MIN;
+    }
+    static uint64_t x86_u64(float f) {
+        if (f < 9223372036854775808.0f) return (uint64_t)x86_64(f);
+        return (uint64_t)x86_64(f - 9223372036854775808.0f) ^ 0x8000000000000000ull;
+    }
+    static int64_t sat_s32(float f) {
+        if (f != f) return 0;
+        if (f >= 2147483648.0f) return INT32_MAX;
+        if (f <= -2147483648.0f) return INT32_MIN;
+        return (int64_t)(int32_t)f;
+    }
+    static uint64_t sat_u32(float f) {
+        if (f != f || f <= -1.0f) return 0;
+        if (f >= 4294967296.0f) return UINT32_MAX;
+        return (uint64_t)(uint32_t)f;
+    }
+    static int64_t sat_s64(float f) {
+        if (f != f) return 0;
+        if (f >= 9223372036854775808.0f) return INT64_MAX;
+        if (f <= -9223372036854775808.0f) return INT64_MIN;
+        return (int64_t)f;
+    }
+    static uint64_t sat_u64(float f) {
+        if (f != f || f <= -1.0f) return 0;
+        if (f >= 18446744073709551616.0f) return UINT64_MAX;
+        return (uint64_t)f;
+    }
+};
+
 template <typename T>
-__host__ __device__ __forceinline__ T eps2_of(float eps) {
+inline T eps2_of(float eps, bool aarch64) {
     const float e2 = eps * eps;
-    if constexpr (Elem<T>::kFloat) return (T)e2;
-    else if constexpr (sizeof(T) < 4) return (T)(int32_t)e2;
-    else if constexpr (std::is_same<T, uint32_t>::value) return (T)(int64_t)e2;
-    else return (T)e2;
+    if constexpr (Elem<T>::kFloat) {
+        return (T)e2;
+    } else if constexpr (std::is_signed<T>::value) {
+        if constexpr (sizeof(T) <= 4) return (T)(aarch64 ? Eps2Conv::sat_s32(e2) : Eps2Conv::x86_32(e2));
+        else return (T)(aarch64 ? Eps2Conv::sat_s64(e2) : Eps2Conv::x86_64(e2));
+    } else {
+        if constexpr (sizeof(T) < 4) return (T)(aarch64 ? (int64_t)Eps2Conv::sat_u32(e2) : Eps2Conv::x86_32(e2));
+        else if constexpr (sizeof(T) == 4) return (T)(aarch64 ? (int64_t)Eps2Conv::sat_u32(e2) : Eps2Conv::x86_64(e2));
+        else return (T)(aarch64 ? Eps2Conv::sat_u64(e2) : Eps2Conv::x86_u64(e2));
+    }
 }
 
 template <typename T>

@@ -58,7 +58,7 @@ int hpd_cluster_device_noalloc(float epsilon, uint64_t min_points, int32_t cell_
         return fail(HPD_ERR_INVALID, "the no-allocation entry point takes at most 32768 points (got " +
                                          std::to_string(n) + ")");
     if (cell_mode != HPD_CELL_RECIP && cell_mode != HPD_CELL_DIV) return fail(HPD_ERR_INVALID, "bad cell mode");
-    if (dist_mode < HPD_DIST_GCC_X86 || dist_mode > HPD_DIST_SEQ_FMA) return fail(HPD_ERR_INVALID, "bad distance mode");
+    if (dist_mode < HPD_DIST_GCC_X86 || dist_mode > HPD_DIST_GCC_AARCH64) return fail(HPD_ERR_INVALID, "bad distance mode");
     if (n == 0) return HPD_OK;
     if (!d_data || !d_labels) return fail(HPD_ERR_INVALID, "null data or label pointer");
     int device = 0;

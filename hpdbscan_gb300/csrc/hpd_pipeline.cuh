@@ -46,14 +46,19 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
             else if ((d) == 3) KERNEL<T, kDistSeq, 3><<<grid, block, smem, stream>>>(__VA_ARGS__);           \
             else KERNEL<T, kDistSeq, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
         } else if ((d) == 2) {                                                                               \
-            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 2><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            /* aarch64: float below 4 dims is the fused running sum; double d = 2 equals the plain sum */   \
+            if ((mode) == kDistSeqFma || ((mode) == kDistGccArm && sizeof(T) == 4))                          \
+                KERNEL<T, kDistSeqFma, 2><<<grid, block, smem, stream>>>(__VA_ARGS__);                    \
             else KERNEL<T, kDistSeq, 2><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
         } else if ((d) == 3) {                                                                               \
-            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 3><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            if ((mode) == kDistSeqFma || ((mode) == kDistGccArm && sizeof(T) == 4))                          \
+                KERNEL<T, kDistSeqFma, 3><<<grid, block, smem, stream>>>(__VA_ARGS__);                    \
+            else if ((mode) == kDistGccArm) KERNEL<T, kDistGccArm, 0><<<grid, block, smem, stream>>>(__VA_ARGS__); \
             else KERNEL<T, kDistSeq, 3><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
         } else {                                                                                             \
             if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 0><<<grid, block, smem, stream>>>(__VA_ARGS__); \
             else if ((mode) == kDistSeq) KERNEL<T, kDistSeq, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);  \
+            else if ((mode) == kDistGccArm) KERNEL<T, kDistGccArm, 0><<<grid, block, smem, stream>>>(__VA_ARGS__); \
             else KERNEL<T, kDistGccX86, 0><<<grid, block, smem, stream>>>(__VA_ARGS__);                      \
         }                                                                                                    \
     } while (0)
@@ -67,14 +72,19 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
             else if ((d) == 3) KERNEL<T, kDistSeq, 3, B><<<grid, block, smem, stream>>>(__VA_ARGS__);           \
             else KERNEL<T, kDistSeq, 0, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
         } else if ((d) == 2) {                                                                               \
-            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 2, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            /* aarch64: float below 4 dims is the fused running sum; double d = 2 equals the plain sum */   \
+            if ((mode) == kDistSeqFma || ((mode) == kDistGccArm && sizeof(T) == 4))                          \
+                KERNEL<T, kDistSeqFma, 2, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                    \
             else KERNEL<T, kDistSeq, 2, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
         } else if ((d) == 3) {                                                                               \
-            if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 3, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            if ((mode) == kDistSeqFma || ((mode) == kDistGccArm && sizeof(T) == 4))                          \
+                KERNEL<T, kDistSeqFma, 3, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                    \
+            else if ((mode) == kDistGccArm) KERNEL<T, kDistGccArm, 0, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
             else KERNEL<T, kDistSeq, 3, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                         \
         } else {                                                                                             \
             if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, 0, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
             else if ((mode) == kDistSeq) KERNEL<T, kDistSeq, 0, B><<<grid, block, smem, stream>>>(__VA_ARGS__);  \
+            else if ((mode) == kDistGccArm) KERNEL<T, kDistGccArm, 0, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
             else KERNEL<T, kDistGccX86, 0, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                      \
         }                                                                                                    \
     } while (0)
@@ -339,7 +349,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     a.ct.pitch = n;
     a.ct.guard = guard;
     a.guard = guard;
-    a.eps2 = eps2_of<T>(rq.eps);  // const float EPS2 = eps * eps (hpdbscan.h:53), converted to T
+    a.eps2 = eps2_of<T>(rq.eps, rq.dist_mode == HPD_DIST_GCC_AARCH64);  // const float EPS2 = eps * eps (hpdbscan.h:53), as T
     a.items = items;
     a.n_items = n_items;
     a.min_points = (int)std::min<uint64_t>(rq.min_points, (uint64_t)n + 1);

@@ -113,6 +113,9 @@ int run_job(WorkerState& ws, hpd_job& j) {
 int validate(const hpd_job* j) {
     if (!j) return fail(HPD_ERR_INVALID, "null job");
     if (!(j->deadline_ms >= 0)) return fail(HPD_ERR_INVALID, "deadline must be >= 0");
+    if (j->cell_mode != HPD_CELL_RECIP && j->cell_mode != HPD_CELL_DIV) return fail(HPD_ERR_INVALID, "bad cell mode");
+    if (j->dist_mode < HPD_DIST_GCC_X86 || j->dist_mode > HPD_DIST_GCC_AARCH64)
+        return fail(HPD_ERR_INVALID, "bad distance mode");
     if (!(j->epsilon > 0.0f)) return fail(HPD_ERR_INVALID, "epsilon needs to be positive");
     if (elem_size(j->dtype) == 0) return fail(HPD_ERR_UNSUPPORTED, "element type not supported by this build");
     if (j->n < 0 || j->n > INT32_MAX - 1 || j->d < 1) return fail(HPD_ERR_INVALID, "bad shape");

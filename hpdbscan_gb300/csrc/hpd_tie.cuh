@@ -126,8 +126,9 @@ __device__ __forceinline__ void mark_dirty_cell(const QueryArgs<T>& a, int c) {
 // candidates in cells dirtied since the previous pass are rescanned: for every
 // other candidate q the query already holds L(p) <= L(q) from an earlier pass.
 // Lower cells are scanned first and the result is published at once; the own
-// cell is then rescanned until no lane of the warp improves, so that chains of
-// improvements inside one chunk settle within this pass.
+// chunk is then closed in registers (each lane offers its value to the higher
+// lanes within eps, in position order), so that chains of improvements inside one
+// chunk settle within this pass.
 template <typename T, int M, int D>
 __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
     if (!in_range(a.guard, item, a.n_items, kGuardItem)) return;
@@ -195,8 +196,9 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
     for (int o = 16; o > 0; o >>= 1) worst0 = max(worst0, __shfl_xor_sync(0xffffffffu, worst0, o));
     visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
         if (own) {
-            // own cell: the lower chunks once, then the warp's own chunk until no
-            // lane improves (at most one round per lane), publishing every round
+            // own cell: the lower chunks once, then the warp's own chunk: every lane
+            // offers its value to the higher lanes of the chunk within eps; taking the
+            // lanes in position order closes the chunk in one pass, in registers
             const bool improved = publish();
             if (!own_dirty && !__any_sync(0xffffffffu, improved)) return true;
             if (!settled()) {
@@ -205,11 +207,20 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
                 for (int o = 16; o > 0; o >>= 1) worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
                 scan_pruned(r, a.ct.start[r], it.y, worst);
             }
-            bool again = !settled();
-            for (int round = 0; again && round < 33; ++round) {
-                publish();
-                scan_range(a, tile, it.y, pend, aux_of, pair, never);
-                again = __any_sync(0xffffffffu, active && myl < published);
+            if (!settled()) {
+                unsigned lower = 0;  // cores of the chunk below this lane within eps
+                auto aux_core = [&](int j) { return (int)a.core[j]; };
+                auto mark = [&](int qi, int u, int is_core) {
+                    if (active && is_core && qi < p && within<T, M, D>(a, q, tile, u)) lower |= 1u << u;
+                };
+                scan_range(a, tile, it.y, pend, aux_core, mark, never);
+                int offer = (p < pend && a.core[p]) ? (active ? myl : ld_volatile(a.lm1 + p)) : INT_MAX;
+                const int cnt = pend - it.y;
+                for (int j = 0; j < cnt; ++j) {
+                    const int vj = __shfl_sync(0xffffffffu, offer, j);
+                    if (((lower >> j) & 1u) && vj < myl) myl = vj;
+                    if (active) offer = myl;
+                }
             }
             publish();
             return true;

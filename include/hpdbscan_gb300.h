@@ -56,9 +56,12 @@ typedef enum {
  * by a running sum (spatial_index.h:751-754); its CMake flags (-Ofast) let the
  * compiler turn the division into a multiply by 1/eps and reassociate the sum.
  * The defaults reproduce GCC -Ofast on x86-64: reciprocal cell coordinates and
- * the SSE2 partial-sum order. */
+ * the SSE2 partial-sum order.  HPD_DIST_GCC_AARCH64 reproduces GCC -Ofast on aarch64
+ * (NEON lanes accumulated with fused multiply-adds, folded pairwise, fused tail); for
+ * the integer element types the distance modes differ only in how EPS2 = (T)(float)
+ * (eps * eps) converts an out-of-range value: x86-64 gives 0x80...0, aarch64 saturates. */
 typedef enum { HPD_CELL_RECIP = 0, HPD_CELL_DIV = 1 } hpd_cell_mode;
-typedef enum { HPD_DIST_GCC_X86 = 0, HPD_DIST_SEQ = 1, HPD_DIST_SEQ_FMA = 2 } hpd_dist_mode;
+typedef enum { HPD_DIST_GCC_X86 = 0, HPD_DIST_SEQ = 1, HPD_DIST_SEQ_FMA = 2, HPD_DIST_GCC_AARCH64 = 3 } hpd_dist_mode;
 
 typedef struct hpd_handle hpd_handle;
 

@@ -112,6 +112,22 @@ static void label_min(int64_t* addr, int64_t v) {
 /* -------------------------------------------------- squared distance, floats */
 
 static float dist2_f32(const float* p, const float* q, int d, int mode) {
+    if (mode == HPDO_DIST_GCC_AARCH64) {
+        /* GCC -Ofast, aarch64 NEON: below 4 dimensions a fused running sum; else 4
+         * lanes accumulate dimensions k = j (mod 4) with fused multiply-adds over the
+         * first d & ~3 dimensions, are folded pairwise as (l0 + l1) + (l2 + l3), and
+         * the remaining dimensions are added with fused multiply-adds. */
+        int nv = d >= 4 ? (d & ~3) : 0, j = 0;
+        float s = 0.0f;
+        if (nv) {
+            float l[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            for (; j < nv; j += 4)
+                for (int k = 0; k < 4; ++k) { float t = p[j + k] - q[j + k]; l[k] = fmaf(t, t, l[k]); }
+            s = (l[0] + l[1]) + (l[2] + l[3]);
+        }
+        for (; j < d; ++j) { float t = p[j] - q[j]; s = fmaf(t, t, s); }
+        return s;
+    }
     if (mode == HPDO_DIST_SEQ) {
         float off = 0.0f;
         for (int k = 0; k < d; ++k) { float t = p[k] - q[k]; float s = t * t; off = off + s; }
@@ -152,6 +168,24 @@ static float dist2_f32(const float* p, const float* q, int d, int mode) {
 }
 
 static double dist2_f64(const double* p, const double* q, int d, int mode) {
+    if (mode == HPDO_DIST_GCC_AARCH64) {
+        /* GCC -Ofast, aarch64 NEON: from 2 dimensions on, 2 lanes accumulate even / odd
+         * dimensions with fused multiply-adds, summed l0 + l1; an odd last dimension is
+         * added with a fused multiply-add. */
+        int nv = d >= 2 ? (d & ~1) : 0, j = 0;
+        double s = 0.0;
+        if (nv) {
+            double l0 = 0.0, l1 = 0.0;
+            for (; j < nv; j += 2) {
+                double t0 = p[j] - q[j], t1 = p[j + 1] - q[j + 1];
+                l0 = fma(t0, t0, l0);
+                l1 = fma(t1, t1, l1);
+            }
+            s = l0 + l1;
+        }
+        for (; j < d; ++j) { double t = p[j] - q[j]; s = fma(t, t, s); }
+        return s;
+    }
     if (mode == HPDO_DIST_SEQ) {
         double off = 0.0;
         for (int k = 0; k < d; ++k) { double t = p[k] - q[k]; double s = t * t; off = off + s; }
@@ -193,6 +227,45 @@ typedef struct {
     int swapped[MAX_DIMS];     /* dimension order, fewest cells first */
     void* sorted;              /* [n * d] points in sorted order */
 } Index;
+
+/* EPS2 = (T)(float)(eps * eps) (hpdbscan.h:53, then region_query's T parameter) as GCC
+ * compiles the float -> integer conversion for the target.  x86-64: cvttss2si with a
+ * 32-bit result for types below 32 bits and for int32, a 64-bit result for uint32 and
+ * int64, and GCC's two-step sequence around 2^63 for uint64; a value out of range gives
+ * the "integer indefinite" 0x80...0.  aarch64: fcvtzs / fcvtzu into a 32-bit register
+ * for types up to 32 bits, a 64-bit one for the 64-bit types; both saturate. */
+static int64_t cvt_x86_32(float f) {
+    return (f > -2147483649.0f && f < 2147483648.0f) ? (int64_t)(int32_t)f : (int64_t)INT32_MIN;
+}
+static int64_t cvt_x86_64(float f) {
+    return (f >= -9223372036854775808.0f && f < 9223372036854775808.0f) ? (int64_t)f : INT64_MIN;
+}
+static uint64_t cvt_x86_u64(float f) {
+    if (f < 9223372036854775808.0f) return (uint64_t)cvt_x86_64(f);
+    return (uint64_t)cvt_x86_64(f - 9223372036854775808.0f) ^ 0x8000000000000000ull;
+}
+static int64_t sat_s32(float f) {
+    if (f != f) return 0;
+    if (f >= 2147483648.0f) return INT32_MAX;
+    if (f <= -2147483648.0f) return INT32_MIN;
+    return (int64_t)(int32_t)f;
+}
+static uint64_t sat_u32(float f) {
+    if (f != f || f <= -1.0f) return 0;
+    if (f >= 4294967296.0f) return UINT32_MAX;
+    return (uint64_t)(uint32_t)f;
+}
+static int64_t sat_s64(float f) {
+    if (f != f) return 0;
+    if (f >= 9223372036854775808.0f) return INT64_MAX;
+    if (f <= -9223372036854775808.0f) return INT64_MIN;
+    return (int64_t)f;
+}
+static uint64_t sat_u64(float f) {
+    if (f != f || f <= -1.0f) return 0;
+    if (f >= 18446744073709551616.0f) return UINT64_MAX;
+    return (uint64_t)f;
+}
 
 typedef int (*within_fn)(const void* pts, int d, int64_t a, int64_t b, const void* eps2, int mode);
 
@@ -504,20 +577,21 @@ int hpd_oracle_cluster(const void* data, int64_t n, int32_t d, int32_t dtype, fl
     memset(&ix, 0, sizeof ix);
     int rc = 0;
     const float eps2f = eps * eps; /* hpdbscan.h:53 */
+    const int arm = dist_mode == HPDO_DIST_GCC_AARCH64;
     union { float f; double g; int8_t i8; int16_t i16; int32_t i32; int64_t i64;
             uint8_t u8; uint16_t u16; uint32_t u32; uint64_t u64; } e2;
     within_fn within = NULL;
     switch (dtype) {
         case HPDO_F32: rc = build_index_f32((const float*)data, n, d, eps, cell_mode, threads, &ix); e2.f = eps2f; within = within_f32; break;
         case HPDO_F64: rc = build_index_f64((const double*)data, n, d, eps, cell_mode, threads, &ix); e2.g = (double)eps2f; within = within_f64; break;
-        case HPDO_I8:  rc = build_index_i8((const int8_t*)data, n, d, eps, cell_mode, threads, &ix); e2.i8 = (int8_t)(int32_t)eps2f; within = within_i8; break;
-        case HPDO_I16: rc = build_index_i16((const int16_t*)data, n, d, eps, cell_mode, threads, &ix); e2.i16 = (int16_t)(int32_t)eps2f; within = within_i16; break;
-        case HPDO_I32: rc = build_index_i32((const int32_t*)data, n, d, eps, cell_mode, threads, &ix); e2.i32 = (int32_t)eps2f; within = within_i32; break;
-        case HPDO_I64: rc = build_index_i64((const int64_t*)data, n, d, eps, cell_mode, threads, &ix); e2.i64 = (int64_t)eps2f; within = within_i64; break;
-        case HPDO_U8:  rc = build_index_u8((const uint8_t*)data, n, d, eps, cell_mode, threads, &ix); e2.u8 = (uint8_t)(int32_t)eps2f; within = within_u8; break;
-        case HPDO_U16: rc = build_index_u16((const uint16_t*)data, n, d, eps, cell_mode, threads, &ix); e2.u16 = (uint16_t)(int32_t)eps2f; within = within_u16; break;
-        case HPDO_U32: rc = build_index_u32((const uint32_t*)data, n, d, eps, cell_mode, threads, &ix); e2.u32 = (uint32_t)(int64_t)eps2f; within = within_u32; break;
-        case HPDO_U64: rc = build_index_u64((const uint64_t*)data, n, d, eps, cell_mode, threads, &ix); e2.u64 = (uint64_t)eps2f; within = within_u64; break;
+        case HPDO_I8:  rc = build_index_i8((const int8_t*)data, n, d, eps, cell_mode, threads, &ix); e2.i8 = (int8_t)(arm ? sat_s32(eps2f) : cvt_x86_32(eps2f)); within = within_i8; break;
+        case HPDO_I16: rc = build_index_i16((const int16_t*)data, n, d, eps, cell_mode, threads, &ix); e2.i16 = (int16_t)(arm ? sat_s32(eps2f) : cvt_x86_32(eps2f)); within = within_i16; break;
+        case HPDO_I32: rc = build_index_i32((const int32_t*)data, n, d, eps, cell_mode, threads, &ix); e2.i32 = (int32_t)(arm ? sat_s32(eps2f) : cvt_x86_32(eps2f)); within = within_i32; break;
+        case HPDO_I64: rc = build_index_i64((const int64_t*)data, n, d, eps, cell_mode, threads, &ix); e2.i64 = arm ? sat_s64(eps2f) : cvt_x86_64(eps2f); within = within_i64; break;
+        case HPDO_U8:  rc = build_index_u8((const uint8_t*)data, n, d, eps, cell_mode, threads, &ix); e2.u8 = (uint8_t)(arm ? (int64_t)sat_u32(eps2f) : cvt_x86_32(eps2f)); within = within_u8; break;
+        case HPDO_U16: rc = build_index_u16((const uint16_t*)data, n, d, eps, cell_mode, threads, &ix); e2.u16 = (uint16_t)(arm ? (int64_t)sat_u32(eps2f) : cvt_x86_32(eps2f)); within = within_u16; break;
+        case HPDO_U32: rc = build_index_u32((const uint32_t*)data, n, d, eps, cell_mode, threads, &ix); e2.u32 = (uint32_t)(arm ? (int64_t)sat_u32(eps2f) : cvt_x86_64(eps2f)); within = within_u32; break;
+        case HPDO_U64: rc = build_index_u64((const uint64_t*)data, n, d, eps, cell_mode, threads, &ix); e2.u64 = arm ? sat_u64(eps2f) : cvt_x86_u64(eps2f); within = within_u64; break;
         default: return fail(2, "unsupported dtype %d", dtype);
     }
     if (rc) return rc;

@@ -41,7 +41,9 @@ enum {
 enum {
     HPDO_DIST_GCC_X86 = 0, /* GCC -Ofast on x86-64/SSE2: lane-strided partial sums, unfused */
     HPDO_DIST_SEQ = 1,     /* strictly sequential, every product and sum rounded */
-    HPDO_DIST_SEQ_FMA = 2  /* strictly sequential, off = fma(t, t, off) */
+    HPDO_DIST_SEQ_FMA = 2, /* strictly sequential, off = fma(t, t, off) */
+    HPDO_DIST_GCC_AARCH64 = 3 /* GCC -Ofast on aarch64/NEON: fused lane sums, pairwise fold,
+                               * fused tail; saturating float -> integer conversions */
 };
 
 int hpd_oracle_cluster(const void* data, int64_t n, int32_t d, int32_t dtype, float eps,

@@ -26,7 +26,7 @@ REF_INCLUDE = os.path.join(REF_ROOT, "include")
 REF_STAGED = os.path.join(HERE, "_ref", "upstream", "include")
 
 CELL_RECIP, CELL_DIV = 0, 1
-DIST_GCC_X86, DIST_SEQ, DIST_SEQ_FMA = 0, 1, 2
+DIST_GCC_X86, DIST_SEQ, DIST_SEQ_FMA, DIST_GCC_AARCH64 = 0, 1, 2, 3
 
 DTYPES = {
     np.dtype(np.float32): 0, np.dtype(np.float64): 1,
