@@ -497,6 +497,15 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         const int kPassesPerCheck = 4;
         const unsigned list_grid = 152 * 16;
         int h_left = h_amb;
+        // the work items holding an unsettled core, in increasing order, into (wl, *wn)
+        auto list_items = [&](int by_value, int* wl, int* wn) -> int {
+            k_tie_list_flags<T><<<blocks_for(n, 256), 256, 0, s>>>(a, by_value);
+            exclusive_scan<uint32_t>(item_flag, item_pos, n_items, scan32, reinterpret_cast<uint32_t*>(wn), s,
+                                     &info.launches);
+            k_tie_compact<<<blocks_for(n_items, 256), 256, 0, s>>>(item_flag, item_pos, n_items, wl, guard);
+            info.launches += 2;
+            return kOk;
+        };
         // round 0 decides with positions as bounds, round 1 with greedy-descent bounds
         for (int round = 0; round < 2 && h_left > 0; ++round) {
             a.amb = lists[cur];
@@ -518,7 +527,12 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
             HPD_QUERY_DISPATCH(k_tie_mark, T, mode, d, blocks_for(h_left, 4), 128, 0, s, a);
             info.launches += 1;
             if (round == 0 && d <= 5) {
-                HPD_QUERY_DISPATCH(k_tie_greedy, T, mode, d, qgrid, 128, qsmem, s, a);
+                // descend from the listed items only (about a tenth of all items)
+                list_items(0, wls[0], wcounts[0]);
+                a.wlist = wls[0];
+                a.n_wlist = wcounts[0];
+                HPD_CU(cudaMemsetAsync(a.ticket, 0, sizeof(int), s));
+                HPD_QUERY_DISPATCH(k_tie_greedy, T, mode, d, list_grid, 128, qsmem, s, a);
                 k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
                 k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
                 info.launches += 3;
@@ -526,12 +540,15 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 break;
             }
         }
-        // relaxation passes until every border is decided or the values are exact
+        // relaxation passes until every border is decided or the values are exact; the
+        // first pass takes the items holding an unsettled core, later passes the items
+        // next to cells whose values dropped
         if (h_left > 0) {
             k_fill_int<<<blocks_for(m, 256), 256, 0, s>>>(cell_min_l, m, INT_MAX);
             k_fill_int<<<blocks_for(n_items, 256), 256, 0, s>>>(item_min_l, n_items, INT_MAX);
             k_tie_cell_min<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
             info.launches += 2;
+            list_items(1, wls[0], wcounts[0]);
         }
         int pass = 0;
         bool converged = false;
@@ -550,8 +567,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 HPD_CU(cudaMemsetAsync(a.n_dlist, 0, sizeof(int), s));
                 HPD_CU(cudaMemsetAsync(a.ticket, 0, sizeof(int), s));
                 if (trace) HPD_CU(cudaMemsetAsync(tcount, 0, 2 * sizeof(unsigned long long), s));
-                if (pass == 1) HPD_QUERY_DISPATCH(k_tie_edge, T, mode, d, qgrid, 128, qsmem, s, a);
-                else HPD_QUERY_DISPATCH(k_tie_edge_list, T, mode, d, list_grid, 128, qsmem, s, a);
+                HPD_QUERY_DISPATCH(k_tie_edge_list, T, mode, d, list_grid, 128, qsmem, s, a);
                 // pointer jumping speeds up the early passes; in the tail few values change
                 // and the edge passes alone reach the same (exact) fixpoint
                 if (pass <= kJumpPasses) k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);

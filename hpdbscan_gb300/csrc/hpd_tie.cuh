@@ -247,13 +247,6 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
     if (__any_sync(0xffffffffu, active && myl < start_l) && lane_id() == 0) mark_dirty_cell(a, r);
 }
 
-template <typename T, int M, int D>
-__global__ void __launch_bounds__(128) k_tie_edge(QueryArgs<T> a) {
-    const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (item >= a.n_items) return;
-    tie_edge_item<T, M, D>(a, item);
-}
-
 // Same pass over a work list (sorted by item, so lower positions go first), by a
 // fixed grid of warps that take the next item from a shared ticket.
 template <typename T, int M, int D>
@@ -362,9 +355,8 @@ static __global__ void k_tie_compact(uint32_t* item_flag, const uint32_t* pos, i
 // from p (pointer jumping) ends at an upper bound of L(p) - 1, equal to the
 // component root whenever the descent reaches it.  Each lane stops at its first hit.
 template <typename T, int M, int D>
-__global__ void __launch_bounds__(128) k_tie_greedy(QueryArgs<T> a) {
-    const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (item >= a.n_items) return;
+__device__ __forceinline__ void tie_greedy_item(const QueryArgs<T>& a, int item) {
+    if (!in_range(a.guard, item, a.n_items, kGuardItem)) return;
     const int2 it = a.items[item];
     const int r = it.x;
     const int pend = min(it.y + 32, a.ct.start[r + 1]);
@@ -403,6 +395,39 @@ __global__ void __launch_bounds__(128) k_tie_greedy(QueryArgs<T> a) {
         });
     }
     if (active) a.lm1[p] = g;
+}
+
+// Greedy descent over the listed work items, by a fixed grid of warps taking the next
+// list entry from a shared ticket.
+template <typename T, int M, int D>
+__global__ void __launch_bounds__(128) k_tie_greedy(QueryArgs<T> a) {
+    int cnt = *a.n_wlist;
+    if (!in_range(a.guard, cnt, (long long)a.n_items + 1, kGuardCount)) cnt = 0;
+    for (;;) {
+        int wi = 0;
+        if (lane_id() == 0) wi = atomicAdd(a.ticket, 1);
+        wi = __shfl_sync(0xffffffffu, wi, 0);
+        if (wi >= cnt) return;
+        tie_greedy_item<T, M, D>(a, a.wlist[wi]);
+    }
+}
+
+// Flags the work items holding a core of a component next to an undecided border,
+// at or below the component's highest such core (tmax), that is not settled yet:
+// its position (by_value 0, before the descent) or its value (by_value 1) is at
+// least the component's threshold.  k_tie_compact lists the flagged items in order.
+template <typename T>
+__global__ void k_tie_list_flags(QueryArgs<T> a, int by_value) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.n || !a.core[p]) return;
+    const int root = a.parent[p];
+    if (!in_range(a.guard, root, a.n, kGuardRoot) || p > a.tmax[root]) return;
+    if ((by_value ? ld_volatile(a.lm1 + p) : p) < a.tlow[root]) return;
+    const int c = (int)a.cellrank[p];
+    if (!in_range(a.guard, c, a.ct.m, kGuardCellRank)) return;
+    const int s0 = a.ct.start[c];
+    const int ti = (int)a.ipos[s0] + ((p - s0) >> 5);
+    if (in_range(a.guard, ti, a.n_items, kGuardItemIndex)) a.item_flag[ti] = 1u;
 }
 
 // Decides the ambiguous borders of the list (a.amb, *a.n_amb) that current bounds
