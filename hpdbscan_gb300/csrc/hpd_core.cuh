@@ -34,6 +34,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
         }
     };
     __shared__ int2 s_rng[4][kMaxRanges];
+    __shared__ int s_pre[4][32];
     const int w = threadIdx.x >> 5;
     const int item = blockIdx.x * 4 + w;
     if (item >= a.n_items) return;
@@ -67,8 +68,9 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
     int S = 1;
     for (int sd = 0; sd < a.g.d; ++sd) S *= 3;
     if (!PRUNE && pend - it.y <= kSparseQueries && S <= kMaxRanges) {
-        // few queries: the whole warp tests consecutive candidates of one query at a
-        // time (a ballot counts the hits), instead of leaving most lanes idle
+        // few queries: the candidates of all neighbour cells form one flat list; each
+        // lane loads one candidate and tests every open query against it (a ballot
+        // counts the hits per query), so a candidate is loaded once for the item
         int nr = 0;
         visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
             if (lane_id() == 0) s_rng[w][nr] = make_int2(a.ct.start[cr], a.ct.start[cr + 1]);
@@ -76,34 +78,53 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
             return true;
         });
         __syncwarp();
-        for (int src = 0; src < pend - it.y; ++src) {
-            T qq[D > 0 ? D : kMaxDims];
+        const int lane = (int)lane_id();
+        const int sz = lane < nr ? s_rng[w][lane].y - s_rng[w][lane].x : 0;
+        int incl = sz;
 #pragma unroll
-            for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-                if (D == 0 && k >= a.g.d) break;
-                qq[k] = shfl_val(q[k], src);
-            }
-            int hits = 0;
-            for (int ri = 0; ri < nr && hits < limit; ++ri) {
-                const int ce = s_rng[w][ri].y;
-                for (int j0 = s_rng[w][ri].x; j0 < ce && hits < limit; j0 += 32) {
-                    const int j = j0 + (int)lane_id();
-                    bool hit = false;
-                    if (j < ce) {
-                        T c[D > 0 ? D : kMaxDims];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        s_pre[w][lane] = incl - sz;  // first flat index of range `lane`
+        __syncwarp();
+        const int nq = pend - it.y;
+        int hits = 0;  // lane i < nq: hits of query i
+        unsigned open = __ballot_sync(0xffffffffu, lane < nq);
+        for (int t0 = 0; t0 < total && open; t0 += 32) {
+            const int t = t0 + lane;
+            const bool valid = t < total;
+            T c[D > 0 ? D : kMaxDims];
+            if (valid) {
+                int lo = 0, hi = nr - 1;  // last range starting at or before t
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s_pre[w][mid] <= t) lo = mid; else hi = mid - 1;
+                }
+                const int j = s_rng[w][lo].x + (t - s_pre[w][lo]);
 #pragma unroll
-                        for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-                            if (D == 0 && k >= a.g.d) break;
-                            c[k] = a.coords[(size_t)k * a.n + j];
-                        }
-                        hit = within_vals<T, M, D>(a, qq, c);
-                        if constexpr (COUNT) ++evals;
-                    }
-                    hits += __popc(__ballot_sync(0xffffffffu, hit));
+                for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                    if (D == 0 && k >= a.g.d) break;
+                    c[k] = a.coords[(size_t)k * a.n + j];
                 }
             }
-            if (lane_id() == 0) a.core[it.y + src] = hits >= limit ? 1 : 0;
+            for (int src = 0; src < nq; ++src) {
+                if (!((open >> src) & 1u)) continue;
+                T qq[D > 0 ? D : kMaxDims];
+#pragma unroll
+                for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
+                    if (D == 0 && k >= a.g.d) break;
+                    qq[k] = shfl_val(q[k], src);
+                }
+                const bool hit = valid && within_vals<T, M, D>(a, qq, c);
+                if constexpr (COUNT) evals += valid ? 1 : 0;
+                const int h = __popc(__ballot_sync(0xffffffffu, hit));
+                if (lane == src) hits += h;
+            }
+            open = __ballot_sync(0xffffffffu, lane < nq && hits < limit);
         }
+        if (lane < nq) a.core[it.y + lane] = hits >= limit ? 1 : 0;
         flush_evals();
         return;
     }
