@@ -231,6 +231,8 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     need += dense_k ? (size_t)dense_max * groups_cap * 2 * d * sizeof(T) : 0;   // sub-cell boxes
     need += dense_k ? (size_t)n * d * sizeof(T) : 0;                 // dense cells' coordinates by sub-cell
     need += (size_t)n * 4;                                           // second ambiguous list
+    const int chunk_cap = n / 8 + 1024;
+    need += (size_t)chunk_cap * 16;                                  // tie-break chunk tasks
     need += (size_t)ncounts * 4 + (size_t)nscan * 8 + 256;           // radix counts, scan scratch, totals, flags
     need += 64 * 256;                                                // alignment of up to 64 blocks
     HPD_CU(main.reserve(need));
@@ -277,11 +279,13 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     T* dense_box = main.take<T>(dense_k ? (size_t)dense_max * groups_cap * 2 * d : 0);
     T* dense_coords = main.take<T>(dense_k ? (size_t)n * d : 0);
     uint32_t* item_pos = main.take<uint32_t>(n);
+    int4* chunks = main.take<int4>(chunk_cap);
     uint32_t* counts = main.take<uint32_t>(ncounts);
     uint32_t* scan32 = main.take<uint32_t>(2 * nscan);
     uint32_t* totals = main.take<uint32_t>(4);   // cells, items, largest cell
     int* flags_dev = main.take<int>(32);          // list counters, [6] cores, [8..11] trace, [12] dense cells,
-                                                  // [13..15] range-check record, [16..17] pair count
+                                                  // [13..15] range-check record, [16..17] pair count,
+                                                  // [18] tie-break chunk tasks
     if (main.overflowed()) {
         err = "internal error: device buffer plan exceeds its reservation";
         return kRuntime;
@@ -486,6 +490,9 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         a.item_min_l = item_min_l;
         a.item_flag = item_flag;
         a.ticket = flags_dev + 5;
+        a.chunks = chunks;
+        a.n_chunks = flags_dev + 18;
+        a.chunk_cap = chunk_cap;
         HPD_CU(cudaMemsetAsync(item_flag, 0, (size_t)n_items * sizeof(uint32_t), s));
         a.gen = 0;
         // ping-pong lists of undecided borders (amb, amb2) and of work items (wl0, wl1)
@@ -567,7 +574,11 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 HPD_CU(cudaMemsetAsync(a.n_dlist, 0, sizeof(int), s));
                 HPD_CU(cudaMemsetAsync(a.ticket, 0, sizeof(int), s));
                 if (trace) HPD_CU(cudaMemsetAsync(tcount, 0, 2 * sizeof(unsigned long long), s));
+                HPD_CU(cudaMemsetAsync(a.n_chunks, 0, sizeof(int), s));
                 HPD_QUERY_DISPATCH(k_tie_edge_list, T, mode, d, list_grid, 128, qsmem, s, a);
+                HPD_CU(cudaMemsetAsync(a.ticket, 0, sizeof(int), s));
+                HPD_QUERY_DISPATCH(k_tie_edge_chunks, T, mode, d, list_grid, 128, qsmem, s, a);
+                info.launches += 1;
                 // pointer jumping speeds up the early passes; in the tail few values change
                 // and the edge passes alone reach the same (exact) fixpoint
                 if (pass <= kJumpPasses) k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);

@@ -206,6 +206,9 @@ struct QueryArgs {
     int* amb_out;         // undecided ambiguous borders after a decision round
     int* n_amb_out;
     unsigned long long* pair_count;  // diagnostic pass: distance evaluations of the core test
+    int4* chunks;         // tie-break chunk tasks (item, cell, first, end position) of a pass
+    int* n_chunks;
+    int chunk_cap;
 };
 
 // Per-warp tile in shared memory: d planes of 32 coordinates plus one aux word.

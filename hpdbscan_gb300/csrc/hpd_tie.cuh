@@ -122,6 +122,27 @@ __device__ __forceinline__ void mark_dirty_cell(const QueryArgs<T>& a, int c) {
     }
 }
 
+constexpr int kInlineTiles = 4;  // tiles a work item scans of one range before handing the rest off
+constexpr int kChunkTiles = 4;   // tiles per chunk task
+
+// Hands [t0, ce) of cell cr, scanned for `item`, to chunk tasks of kChunkTiles tiles
+// (warp-uniform; false when the queue is full, and the caller scans on itself).
+template <typename T>
+__device__ __forceinline__ bool push_chunks(const QueryArgs<T>& a, int item, int cr, int t0, int ce) {
+    const int span = 32 * kChunkTiles;
+    const int nt = (ce - t0 + span - 1) / span;
+    int k = 0;
+    if (lane_id() == 0) {
+        k = atomicAdd(a.n_chunks, nt);
+        if (k + nt > a.chunk_cap) k = -1;
+    }
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k < 0) return false;
+    for (int i = (int)lane_id(); i < nt; i += 32)
+        a.chunks[k + i] = make_int4(item, cr, t0 + i * span, min(t0 + (i + 1) * span, ce));
+    return true;
+}
+
 // One relaxation pass over decreasing core edges for one work item.  Only
 // candidates in cells dirtied since the previous pass are rescanned: for every
 // other candidate q the query already holds L(p) <= L(q) from an earlier pass.
@@ -179,13 +200,20 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
     auto settled = [&]() { return __all_sync(0xffffffffu, !active || myl < tl); };
     // tiles are aligned with the 32-point chunks of a cell, so each tile is one work
     // item; a tile whose smallest value cannot improve any lane is skipped unread
+    // Long scans (cells of hundreds of points) would keep one warp busy while the rest
+    // of the grid idles: after kInlineTiles tiles the rest of the range is handed to
+    // chunk tasks (k_tie_edge_chunks), whose results are published by atomicMin like
+    // this item's own.
     auto scan_pruned = [&](int cr, int cs, int ce, int worst) {
         const int first_item = (int)a.ipos[a.ct.start[cr]];
+        int scanned = 0;
         for (int t0 = cs; t0 < ce; t0 += 32) {
+            if (scanned == kInlineTiles && a.chunks && push_chunks(a, item, cr, t0, ce)) return false;
             const int ti = first_item + ((t0 - a.ct.start[cr]) >> 5);
             if (!in_range(a.guard, ti, a.n_items, kGuardItemIndex)) return false;
             if (ld_volatile(a.item_min_l + ti) >= worst) continue;
             if (a.trace_counts && lane_id() == 0) atomicAdd(a.trace_counts + 1, 1ull);
+            ++scanned;
             if (scan_range(a, tile, t0, min(t0 + 32, ce), aux_of, pair, settled)) return true;
         }
         return false;
@@ -259,6 +287,71 @@ __global__ void __launch_bounds__(128) k_tie_edge_list(QueryArgs<T> a) {
         wi = __shfl_sync(0xffffffffu, wi, 0);
         if (wi >= cnt) return;
         tie_edge_item<T, M, D>(a, a.wlist[wi]);
+    }
+}
+
+// One chunk task: the lanes of a work item against the tiles [t0, t1) of cell cr, as
+// in tie_edge_item; improvements are published by atomicMin and dirty the item's cell.
+template <typename T, int M, int D>
+__device__ __forceinline__ void tie_edge_chunk(const QueryArgs<T>& a, int4 task) {
+    const int item = task.x, cr = task.y;
+    if (!in_range(a.guard, item, a.n_items, kGuardItem) || !in_range(a.guard, cr, a.ct.m, kGuardCellRank)) return;
+    const int2 it = a.items[item];
+    const int r = it.x;
+    if (!in_range(a.guard, r, a.ct.m, kGuardCellRank) || !in_range(a.guard, it.y, a.n, kGuardItem)) return;
+    const int pend = min(it.y + 32, a.ct.start[r + 1]);
+    const int p = it.y + (int)lane_id();
+    bool active = p < pend && a.core[p];
+    const int root = active ? a.parent[p] : INT_MIN;
+    if (active && !in_range(a.guard, root, a.n, kGuardRoot)) active = false;
+    int tl = INT_MIN;
+    if (active) {
+        tl = a.tlow[root];
+        active = p <= a.tmax[root] && ld_volatile(a.lm1 + p) >= tl;
+    }
+    if (!__any_sync(0xffffffffu, active)) return;
+    const Tile<T> tile = warp_tile<T>(a.g.d);
+    T q[D > 0 ? D : kMaxDims];
+    load_query<T, D>(a, p, active, q);
+    const int start_l = active ? ld_volatile(a.lm1 + p) : INT_MAX;
+    int myl = start_l;
+    auto aux_of = [&](int j) { return a.core[j] ? ld_volatile(a.lm1 + j) : INT_MAX; };
+    auto pair = [&](int qi, int u, int lq) {
+        if (!active || lq >= myl || qi >= p) return;
+        if (within<T, M, D>(a, q, tile, u)) myl = lq;
+    };
+    auto settled = [&]() { return __all_sync(0xffffffffu, !active || myl < tl); };
+    int worst = (active && myl >= tl) ? myl : INT_MIN;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+    const int c0 = a.ct.start[cr];
+    const int first_item = (int)a.ipos[c0];
+    for (int t0 = task.z; t0 < task.w; t0 += 32) {
+        const int ti = first_item + ((t0 - c0) >> 5);
+        if (!in_range(a.guard, ti, a.n_items, kGuardItemIndex)) break;
+        if (ld_volatile(a.item_min_l + ti) >= worst) continue;
+        if (scan_range(a, tile, t0, min(t0 + 32, task.w), aux_of, pair, settled)) break;
+    }
+    const bool better = active && myl < start_l;
+    if (better) {
+        atomicMin(a.lm1 + p, myl);
+        atomicMin(a.cell_min_l + r, myl);
+        atomicMin(a.item_min_l + item, myl);
+    }
+    if (__any_sync(0xffffffffu, better) && lane_id() == 0) mark_dirty_cell(a, r);
+}
+
+// The chunk tasks of a pass, by a fixed grid of warps taking the next task by ticket.
+template <typename T, int M, int D>
+__global__ void __launch_bounds__(128) k_tie_edge_chunks(QueryArgs<T> a) {
+    int cnt = *a.n_chunks;
+    if (cnt > a.chunk_cap) cnt = a.chunk_cap;
+    for (;;) {
+        int wi = 0;
+        if (lane_id() == 0) wi = atomicAdd(a.ticket, 1);
+        wi = __shfl_sync(0xffffffffu, wi, 0);
+        if (wi >= cnt) return;
+        tie_edge_chunk<T, M, D>(a, a.chunks[wi]);
     }
 }
 
