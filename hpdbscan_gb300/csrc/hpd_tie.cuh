@@ -123,7 +123,37 @@ __device__ __forceinline__ void mark_dirty_cell(const QueryArgs<T>& a, int c) {
 }
 
 constexpr int kInlineTiles = 4;  // tiles a work item scans of one range before handing the rest off
-constexpr int kChunkTiles = 4;   // tiles per chunk task
+constexpr int kChunkTiles = 32;  // tiles per chunk task (one check of their minima)
+
+// Scans the tiles of [c0, c1) (a range of cell cr, tiles aligned with its 32-point
+// work items) whose item minimum is below `worst`, 32 tiles per check of the minima:
+// scan(t0, t1) per surviving tile, in order.  Stops after `budget` scanned tiles and
+// returns the first position not examined (c1 when done), or -1 when scan says stop.
+template <typename T, class Scan>
+__device__ __forceinline__ int scan_live_tiles(const QueryArgs<T>& a, int cr, int c0, int c1, int worst, int budget,
+                                               Scan&& scan) {
+    const int cs = a.ct.start[cr];
+    const int first = (int)a.ipos[cs];
+    int scanned = 0;
+    for (int base = c0; base < c1; base += 32 * 32) {
+        const int t = base + 32 * (int)lane_id();
+        bool live = false;
+        if (t < c1) {
+            const int ti = first + ((t - cs) >> 5);
+            live = in_range(a.guard, ti, a.n_items, kGuardItemIndex) && ld_volatile(a.item_min_l + ti) < worst;
+        }
+        unsigned mask = __ballot_sync(0xffffffffu, live);
+        while (mask) {
+            const int u = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int t0 = base + 32 * u;
+            if (scanned == budget) return t0;
+            ++scanned;
+            if (scan(t0, min(t0 + 32, c1))) return -1;
+        }
+    }
+    return c1;
+}
 
 // Hands [t0, ce) of cell cr, scanned for `item`, to chunk tasks of kChunkTiles tiles
 // (warp-uniform; false when the queue is full, and the caller scans on itself).
@@ -205,18 +235,16 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
     // chunk tasks (k_tie_edge_chunks), whose results are published by atomicMin like
     // this item's own.
     auto scan_pruned = [&](int cr, int cs, int ce, int worst) {
-        const int first_item = (int)a.ipos[a.ct.start[cr]];
-        int scanned = 0;
-        for (int t0 = cs; t0 < ce; t0 += 32) {
-            if (scanned == kInlineTiles && a.chunks && push_chunks(a, item, cr, t0, ce)) return false;
-            const int ti = first_item + ((t0 - a.ct.start[cr]) >> 5);
-            if (!in_range(a.guard, ti, a.n_items, kGuardItemIndex)) return false;
-            if (ld_volatile(a.item_min_l + ti) >= worst) continue;
+        auto scan = [&](int t0, int t1) {
             if (a.trace_counts && lane_id() == 0) atomicAdd(a.trace_counts + 1, 1ull);
-            ++scanned;
-            if (scan_range(a, tile, t0, min(t0 + 32, ce), aux_of, pair, settled)) return true;
+            return scan_range(a, tile, t0, t1, aux_of, pair, settled);
+        };
+        int rest = scan_live_tiles(a, cr, cs, ce, worst, a.chunks ? kInlineTiles : INT_MAX, scan);
+        while (rest >= 0 && rest < ce) {
+            if (push_chunks(a, item, cr, rest, ce)) return false;
+            rest = scan_live_tiles(a, cr, rest, ce, worst, INT_MAX, scan);  // queue full: on our own
         }
-        return false;
+        return rest < 0;
     };
     const bool own_dirty = ld_volatile(a.dirty_gen + r) >= since;
     int worst0 = active ? myl : INT_MIN;  // largest lane value at the start: a cell must beat it
@@ -324,14 +352,8 @@ __device__ __forceinline__ void tie_edge_chunk(const QueryArgs<T>& a, int4 task)
     int worst = (active && myl >= tl) ? myl : INT_MIN;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
-    const int c0 = a.ct.start[cr];
-    const int first_item = (int)a.ipos[c0];
-    for (int t0 = task.z; t0 < task.w; t0 += 32) {
-        const int ti = first_item + ((t0 - c0) >> 5);
-        if (!in_range(a.guard, ti, a.n_items, kGuardItemIndex)) break;
-        if (ld_volatile(a.item_min_l + ti) >= worst) continue;
-        if (scan_range(a, tile, t0, min(t0 + 32, task.w), aux_of, pair, settled)) break;
-    }
+    scan_live_tiles(a, cr, task.z, task.w, worst, INT_MAX,
+                    [&](int t0, int t1) { return scan_range(a, tile, t0, t1, aux_of, pair, settled); });
     const bool better = active && myl < start_l;
     if (better) {
         atomicMin(a.lm1 + p, myl);
