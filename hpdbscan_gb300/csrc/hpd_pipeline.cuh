@@ -231,7 +231,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     need += dense_k ? (size_t)dense_max * groups_cap * 2 * d * sizeof(T) : 0;   // sub-cell boxes
     need += dense_k ? (size_t)n * d * sizeof(T) : 0;                 // dense cells' coordinates by sub-cell
     need += (size_t)n * 4;                                           // second ambiguous list
-    const int chunk_cap = n / 8 + 1024;
+    const int chunk_cap = n / 4 + 1024;
     need += (size_t)chunk_cap * 16;                                  // tie-break chunk tasks
     need += (size_t)ncounts * 4 + (size_t)nscan * 8 + 256;           // radix counts, scan scratch, totals, flags
     need += 64 * 256;                                                // alignment of up to 64 blocks

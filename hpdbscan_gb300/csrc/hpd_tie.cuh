@@ -123,7 +123,7 @@ __device__ __forceinline__ void mark_dirty_cell(const QueryArgs<T>& a, int c) {
 }
 
 constexpr int kInlineTiles = 4;  // tiles a work item scans of one range before handing the rest off
-constexpr int kChunkTiles = 32;  // tiles per chunk task (one check of their minima)
+constexpr int kChunkTiles = 16;  // tiles per chunk task (one check of their minima)
 
 // Scans the tiles of [c0, c1) (a range of cell cr, tiles aligned with its 32-point
 // work items) whose item minimum is below `worst`, 32 tiles per check of the minima:
@@ -162,12 +162,14 @@ __device__ __forceinline__ bool push_chunks(const QueryArgs<T>& a, int item, int
     const int span = 32 * kChunkTiles;
     const int nt = (ce - t0 + span - 1) / span;
     int k = 0;
-    if (lane_id() == 0) {
-        k = atomicAdd(a.n_chunks, nt);
-        if (k + nt > a.chunk_cap) k = -1;
-    }
+    if (lane_id() == 0) k = atomicAdd(a.n_chunks, nt);
     k = __shfl_sync(0xffffffffu, k, 0);
-    if (k < 0) return false;
+    if (k + nt > a.chunk_cap) {
+        // the queue is full: the slots of [k, k + nt) below the cap become no-op tasks,
+        // so that the chunk kernel reads no unwritten slot, and the caller scans on
+        for (int i = (int)lane_id(); i < nt && k + i < a.chunk_cap; i += 32) a.chunks[k + i] = make_int4(-1, 0, 0, 0);
+        return false;
+    }
     for (int i = (int)lane_id(); i < nt; i += 32)
         a.chunks[k + i] = make_int4(item, cr, t0 + i * span, min(t0 + (i + 1) * span, ce));
     return true;
@@ -323,6 +325,7 @@ __global__ void __launch_bounds__(128) k_tie_edge_list(QueryArgs<T> a) {
 template <typename T, int M, int D>
 __device__ __forceinline__ void tie_edge_chunk(const QueryArgs<T>& a, int4 task) {
     const int item = task.x, cr = task.y;
+    if (item < 0) return;  // no-op slot of a push that found the queue full
     if (!in_range(a.guard, item, a.n_items, kGuardItem) || !in_range(a.guard, cr, a.ct.m, kGuardCellRank)) return;
     const int2 it = a.items[item];
     const int r = it.x;
@@ -366,8 +369,9 @@ __device__ __forceinline__ void tie_edge_chunk(const QueryArgs<T>& a, int4 task)
 // The chunk tasks of a pass, by a fixed grid of warps taking the next task by ticket.
 template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_tie_edge_chunks(QueryArgs<T> a) {
-    int cnt = *a.n_chunks;
+    int cnt = *a.n_chunks;  // may exceed chunk_cap after a full queue: slots stop there
     if (cnt > a.chunk_cap) cnt = a.chunk_cap;
+    if (cnt < 0) cnt = 0;
     for (;;) {
         int wi = 0;
         if (lane_id() == 0) wi = atomicAdd(a.ticket, 1);
