@@ -91,7 +91,7 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
 
 constexpr int kDenseMinPoints = 128;  // cells with this many points take the dense-cell path
 constexpr int kFineMinPoints = 65536;  // a largest cell this big selects the finer sub-cell split
-constexpr int kJumpPasses = 8;          // relaxation passes followed by a pointer-jumping sweep
+constexpr int kJumpPasses = 3;          // relaxation passes followed by a pointer-jumping sweep
 
 template <typename T, typename K>
 int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, std::string& err, const Grid& g,
@@ -582,11 +582,9 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 // pointer jumping speeds up the early passes; in the tail few values change
                 // and the edge passes alone reach the same (exact) fixpoint
                 if (pass <= kJumpPasses) k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
+                HPD_CU(cudaMemsetAsync(a.n_wlist_out, 0, sizeof(int), s));
                 k_tie_schedule<T><<<list_grid, 128, 0, s>>>(a);
-                exclusive_scan<uint32_t>(item_flag, item_pos, n_items, scan32,
-                                         reinterpret_cast<uint32_t*>(a.n_wlist_out), s, &info.launches);
-                k_tie_compact<<<blocks_for(n_items, 256), 256, 0, s>>>(item_flag, item_pos, n_items, a.wlist_out, guard);
-                info.launches += 4;
+                info.launches += 3;
                 if (trace) {
                     unsigned long long tc[2];
                     int wn = 0;

@@ -427,8 +427,7 @@ __global__ void k_tie_cell_min(QueryArgs<T> a) {
 }
 
 // Next pass's work: the items of every cell whose lower stencil or own cell was
-// dirtied in this pass are flagged (warp per dirty cell); k_tie_compact then lists the
-// flagged items in increasing order.
+// dirtied in this pass are appended to the next work list (warp per dirty cell).
 template <typename T>
 __global__ void __launch_bounds__(128) k_tie_schedule(QueryArgs<T> a) {
     const int nw = gridDim.x * 4;
@@ -448,8 +447,22 @@ __global__ void __launch_bounds__(128) k_tie_schedule(QueryArgs<T> a) {
             const int s0 = a.ct.start[cr];
             const int nit = (a.ct.start[cr + 1] - s0 + 31) >> 5;
             const int first = (int)a.ipos[s0];
-            for (int k = (int)lane; k < nit; k += 32)
-                if (in_range(a.guard, first + k, a.n_items, kGuardItemIndex)) a.item_flag[first + k] = 1u;
+            // append each item once per pass (the stamp gen + 2 marks it listed); the order
+            // of the list does not matter for the relaxation
+            const unsigned stamp = (unsigned)a.gen + 2u;
+            for (int k0 = 0; k0 < nit; k0 += 32) {
+                const int k = k0 + (int)lane;
+                const bool add = k < nit && in_range(a.guard, first + k, a.n_items, kGuardItemIndex) &&
+                                 atomicExch(a.item_flag + first + k, stamp) != stamp;
+                const unsigned m = __ballot_sync(0xffffffffu, add);
+                int base = 0;
+                if (lane == 0 && m) base = atomicAdd(a.n_wlist_out, __popc(m));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (add) {
+                    const int slot = base + __popc(m & ((1u << lane) - 1u));
+                    if (in_range(a.guard, slot, a.n_items, kGuardList)) a.wlist_out[slot] = first + k;
+                }
+            }
             return true;
         }, false, [&](int cr) {
             const int rep_c = a.cell_rep[cr];
