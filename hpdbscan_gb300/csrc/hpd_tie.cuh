@@ -437,13 +437,20 @@ __global__ void __launch_bounds__(128) k_tie_schedule(QueryArgs<T> a) {
     for (int w = blockIdx.x * 4 + (threadIdx.x >> 5); w < cnt; w += nw) {
         const int c = a.dlist[w];
         if (!in_range(a.guard, c, a.ct.m, kGuardDirtyCell)) continue;
-        visit_stencil(a.g, a.ct, c, 2, [&](int cr, bool) {
+        // a cell is relevant when it holds a core of a component below its highest core
+        // next to an undecided border; the first warp to claim it in this pass lists it
+        auto claim = [&](int cr) {
             const int rep_c = a.cell_rep[cr];
-            if (rep_c == kNoCore) return true;
-            if ((a.cell_flags[cr] & kCellUniform) && tmax_of(a, rep_c) < a.ct.start[cr]) return true;
-            int fresh = 0;
-            if (lane == 0) fresh = atomicMax(a.sched_gen + cr, a.gen) < a.gen;
-            if (!__shfl_sync(0xffffffffu, fresh, 0)) return true;
+            if (rep_c == kNoCore) return false;
+            if ((a.cell_flags[cr] & kCellUniform) && tmax_of(a, rep_c) < a.ct.start[cr]) return false;
+            return atomicMax(a.sched_gen + cr, a.gen) < a.gen;
+        };
+        visit_stencil(a.g, a.ct, c, 2, [&](int cr, bool own) {
+            if (own) {  // the stencil filter (claim, one neighbour per lane) skips the own cell
+                int fresh = 0;
+                if (lane == 0) fresh = claim(cr);
+                if (!__shfl_sync(0xffffffffu, fresh, 0)) return true;
+            }
             const int s0 = a.ct.start[cr];
             const int nit = (a.ct.start[cr + 1] - s0 + 31) >> 5;
             const int first = (int)a.ipos[s0];
@@ -464,11 +471,7 @@ __global__ void __launch_bounds__(128) k_tie_schedule(QueryArgs<T> a) {
                 }
             }
             return true;
-        }, false, [&](int cr) {
-            const int rep_c = a.cell_rep[cr];
-            if (rep_c == kNoCore) return false;
-            return !((a.cell_flags[cr] & kCellUniform) && tmax_of(a, rep_c) < a.ct.start[cr]);
-        });
+        }, false, claim);
     }
 }
 
@@ -481,6 +484,8 @@ static __global__ void k_tie_compact(uint32_t* item_flag, const uint32_t* pos, i
         item_flag[i] = 0u;
     }
 }
+
+constexpr int kGreedyTiles = 6;  // tiles a work item of the greedy descent scans at most
 
 // Greedy descent step: g(p) = some core eps-neighbour below p (p itself if none).
 // Any decreasing core edge leads to a position reachable from p, so following g
@@ -510,7 +515,10 @@ __device__ __forceinline__ void tie_greedy_item(const QueryArgs<T>& a, int item)
         if (found || !is_core || qi >= p) return;
         if (within<T, M, D>(a, q, tile, u)) { g = qi; found = true; }
     };
-    auto done = [&]() { return __all_sync(0xffffffffu, found); };
+    // the descent is a bound, not a result: a warp stops after kGreedyTiles tiles, and a
+    // lane without a hit by then keeps its own position (values only need to be reachable)
+    int tiles = 0;
+    auto done = [&]() { return ++tiles >= kGreedyTiles || __all_sync(0xffffffffu, found); };
     // lower positions of the own cell first (most pairs inside a cell are within eps),
     // then the lower face across the most significant dimension, then the rest
     bool all = scan_range(a, tile, a.ct.start[r], pend, aux_of, pair, done);

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(128) k_union_cells(QueryArgs<T> a) {
     visit_stencil(a.g, a.ct, c, 1, [&](int cr, bool own) {
         if (own) return true;
         const int rep_n = a.cell_rep[cr];
-        if (same_component(a.parent, rep_c, rep_n)) return true;
+        if (same_component(a.parent, rep_c, rep_n)) return true;  // joined since the filter ran
         const int ns = a.ct.start[cr], ne = a.ct.start[cr + 1];
         bool joined = false;
         for (int x0 = cs; x0 < ce && !joined; x0 += 32) {
@@ -150,7 +150,11 @@ __global__ void __launch_bounds__(128) k_union_cells(QueryArgs<T> a) {
             }
         }
         return true;
-    }, false, [&](int cr) { return a.cell_rep[cr] != kNoCore && (a.cell_flags[cr] & kCellUniform); });
+    }, false, [&](int cr) {
+        // one neighbour per lane: single-component neighbours not yet in this component
+        const int rep_n = a.cell_rep[cr];
+        return rep_n != kNoCore && (a.cell_flags[cr] & kCellUniform) && uf_find(a.parent, rep_c) != uf_find(a.parent, rep_n);
+    });
 }
 
 // Every core points at its component root; counts the cores (one atomic per warp).
