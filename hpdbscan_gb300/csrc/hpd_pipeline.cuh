@@ -440,7 +440,9 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         HPD_QUERY_DISPATCH(k_dense_pairs, T, mode, d, blocks_for(dense_max, 4), 128, 0, s, a, da);
         info.launches += 3;
     }
+    HPD_QUERY_DISPATCH(k_union_small_cells, T, mode, d, blocks_for(m, 4), 128, qsmem, s, a);
     HPD_QUERY_DISPATCH(k_union_intra, T, mode, d, qgrid, 128, qsmem, s, a);
+    info.launches += 1;
     k_fill_int<<<blocks_for(m, 256), 256, 0, s>>>(cell_rep, m, kNoCore);
     k_cell_rep<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep);
     k_cell_uniform<<<blocks_for(n, 256), 256, 0, s>>>(core, parent, rank, n, cell_rep, cell_flags);

@@ -13,6 +13,65 @@ namespace hpd {
 // core or whose cores are already in the query cell's component.  Within a tile,
 // candidates already in the query's component are skipped without a distance test.
 
+constexpr int kSmallCell = 128;  // cells up to this size are united in shared memory (k_union_small_cells)
+
+// Pairs inside one cell of at most kSmallCell points, one warp per cell: a union-find
+// over the cell's points in shared memory (roots are the smallest local index), then
+// every core's global parent is set to its local root, a core of the same component
+// at a lower position.  No global atomics.
+template <typename T, int M, int D>
+__global__ void __launch_bounds__(128) k_union_small_cells(QueryArgs<T> a) {
+    __shared__ int s_lp[4][kSmallCell];
+    const int w = threadIdx.x >> 5;
+    const int c = blockIdx.x * 4 + w;
+    if (c >= a.ct.m) return;
+    const int cs = a.ct.start[c];
+    const int size = a.ct.start[c + 1] - cs;
+    if (size < 2 || size > kSmallCell) return;
+    if (a.dense_id && a.dense_id[c] >= 0) return;  // connected by the dense-cell kernels
+    const unsigned lane = lane_id();
+    volatile int* lp = s_lp[w];
+    for (int k = (int)lane; k < size; k += 32) lp[k] = k;
+    __syncwarp();
+    auto find = [&](int x) {
+        for (;;) {
+            const int px = lp[x];
+            if (px == x) return x;
+            const int gx = lp[px];
+            if (gx != px) lp[x] = gx;  // path halving
+            x = px;
+        }
+    };
+    auto unite = [&](int x, int y) {
+        for (;;) {
+            x = find(x);
+            y = find(y);
+            if (x == y) return;
+            if (x < y) { const int t = x; x = y; y = t; }
+            if (atomicCAS((int*)&lp[x], x, y) == x) return;
+        }
+    };
+    const Tile<T> tile = warp_tile<T>(a.g.d);
+    for (int i0 = 0; i0 < size; i0 += 32) {
+        const int li = i0 + (int)lane;
+        const int p = cs + li;
+        const bool active = li < size && a.core[p];
+        T q[D > 0 ? D : kMaxDims];
+        load_query<T, D>(a, p, active, q);
+        auto aux_of = [&](int j) { return (int)a.core[j]; };
+        auto pair = [&](int qi, int u, int is_core) {
+            if (active && is_core && qi < p && within<T, M, D>(a, q, tile, u)) unite(li, qi - cs);
+        };
+        auto never = []() { return false; };
+        scan_range(a, tile, cs, min(cs + i0 + 32, cs + size), aux_of, pair, never);
+    }
+    __syncwarp();
+    for (int k = (int)lane; k < size; k += 32)
+        if (a.core[cs + k]) a.parent[cs + k] = cs + find(k);
+}
+
+// Pairs inside the cells larger than kSmallCell that the dense-cell kernels do not
+// connect, one warp per work item.
 template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_union_intra(QueryArgs<T> a) {
     const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
@@ -20,6 +79,7 @@ __global__ void __launch_bounds__(128) k_union_intra(QueryArgs<T> a) {
     const int2 it = a.items[item];
     const int r = it.x;
     if (a.dense_id && a.dense_id[r] >= 0) return;  // connected by the dense-cell kernels
+    if (a.ct.start[r + 1] - a.ct.start[r] <= kSmallCell) return;  // k_union_small_cells
     const int pend = min(it.y + 32, a.ct.start[r + 1]);
     const int p = it.y + (int)lane_id();
     const bool active = p < pend && a.core[p];
