@@ -21,6 +21,7 @@ DIAG_COUNT_PAIRS = 1
 INJECT_FAIL_ALLOC = 1
 
 EXPORTS = ("hpd_create", "hpd_destroy", "hpd_set_arith", "hpd_set_tie_break", "hpd_set_tie_pass_limit",
+           "hpd_set_tuning", "hpd_set_tuning_table",
            "hpd_set_diagnostics", "hpd_debug_inject", "hpd_cluster", "hpd_cluster_device",
            "hpd_get_stats", "hpd_last_error", "hpd_version", "hpd_cluster_device_noalloc",
            "hpd_noalloc_last_error", "hpd_cluster_batch", "hpd_server_create", "hpd_server_submit",
@@ -33,6 +34,16 @@ class Job(ctypes.Structure):
                 ("epsilon", ctypes.c_float), ("min_points", ctypes.c_uint64), ("cell_mode", ctypes.c_int32),
                 ("dist_mode", ctypes.c_int32), ("labels", ctypes.c_void_p), ("status", ctypes.c_int32),
                 ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("deadline_ms", ctypes.c_double)]
+
+
+class Tuning(ctypes.Structure):
+    """hpd_tuning of include/hpdbscan_gb300.h (0: built-in default)."""
+    _fields_ = [("sparse_queries", ctypes.c_int32), ("dense_min_points", ctypes.c_int32),
+                ("greedy_tiles", ctypes.c_int32)]
+
+
+class TuningEntry(ctypes.Structure):
+    _fields_ = [("max_points", ctypes.c_int64), ("dims", ctypes.c_int32), ("tuning", Tuning)]
 
 
 class Stats(ctypes.Structure):
@@ -75,6 +86,10 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     for name in ("hpd_set_tie_pass_limit", "hpd_set_diagnostics", "hpd_debug_inject"):
         getattr(lib, name).argtypes = [H, ctypes.c_int32]
         getattr(lib, name).restype = ctypes.c_int
+    lib.hpd_set_tuning.argtypes = [H, ctypes.POINTER(Tuning)]
+    lib.hpd_set_tuning.restype = ctypes.c_int
+    lib.hpd_set_tuning_table.argtypes = [ctypes.POINTER(TuningEntry), ctypes.c_int32]
+    lib.hpd_set_tuning_table.restype = ctypes.c_int
     lib.hpd_cluster.argtypes = [H, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                 ctypes.c_void_p]
     lib.hpd_cluster.restype = ctypes.c_int

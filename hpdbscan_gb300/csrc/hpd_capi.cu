@@ -19,6 +19,7 @@ struct hpd_handle {
     int tie_mode = HPD_TIE_EXACT;
     int tie_pass_limit = kDefaultTiePassLimit;
     int diag = 0;    // hpd_diag bits
+    hpd_tuning tuning = {0, 0, 0};
     int inject = 0;  // hpd_inject bits for the next call
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -69,6 +70,7 @@ int run(hpd_handle* h, const void* d_data, int64_t n, int32_t d, int32_t dtype, 
     rq.stream = s;
     rq.tie_pass_limit = h->tie_pass_limit;
     rq.count_pairs = (h->diag & HPD_DIAG_COUNT_PAIRS) != 0;
+    rq.tuning = h->tuning;
     std::string err;
     int rc;
     switch (dtype) {
@@ -159,6 +161,25 @@ int hpd_set_tie_pass_limit(hpd_handle* h, int32_t passes) {
     if (!h) return fail(HPD_ERR_INVALID, "null handle");
     if (passes < 0) return fail(HPD_ERR_INVALID, "pass limit must be >= 0");
     h->tie_pass_limit = passes == 0 ? kDefaultTiePassLimit : passes;
+    return HPD_OK;
+}
+
+int hpd_set_tuning(hpd_handle* h, const hpd_tuning* tuning) {
+    if (!h) return fail(HPD_ERR_INVALID, "null handle");
+    if (!tuning) {
+        h->tuning = hpd_tuning{0, 0, 0};
+        return HPD_OK;
+    }
+    if (tuning->sparse_queries < 0 || tuning->sparse_queries > 32 || tuning->dense_min_points < 0 ||
+        (tuning->dense_min_points > 0 && tuning->dense_min_points < 32) || tuning->greedy_tiles < 0)
+        return fail(HPD_ERR_INVALID, "tuning out of range");
+    h->tuning = *tuning;
+    return HPD_OK;
+}
+
+int hpd_set_tuning_table(const hpd_tuning_entry* entries, int32_t n_entries) {
+    if (set_tuning_table(entries, n_entries) != HPD_OK)
+        return fail(HPD_ERR_INVALID, "tuning table: at most 64 entries, non-null when not empty");
     return HPD_OK;
 }
 

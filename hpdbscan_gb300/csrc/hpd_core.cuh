@@ -14,7 +14,6 @@ __device__ __forceinline__ T shfl_val(T v, int src) {
     else return __shfl_sync(0xffffffffu, v, src);
 }
 
-constexpr int kSparseQueries = 8;  // items with at most this many points use candidate lanes
 constexpr int kMaxRanges = 32;     // neighbour ranges kept in shared memory (3^d <= 32: d <= 3)
 
 // F: bit 0 (kCorePrune) selects the cells next to big dense cells, bit 1
@@ -67,7 +66,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
     }
     int S = 1;
     for (int sd = 0; sd < a.g.d; ++sd) S *= 3;
-    if (!PRUNE && pend - it.y <= kSparseQueries && S <= kMaxRanges) {
+    if (!PRUNE && pend - it.y <= a.sparse_queries && S <= kMaxRanges) {
         // few queries: the candidates of all neighbour cells form one flat list; each
         // lane loads one candidate and tests every open query against it (a ballot
         // counts the hits per query), so a candidate is loaded once for the item

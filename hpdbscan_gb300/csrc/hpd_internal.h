@@ -66,7 +66,15 @@ struct Request {
     bool no_dense = false;  // look cells up by binary search only (no grid-sized table)
     int tie_pass_limit = kDefaultTiePassLimit;  // relaxation passes before HPD_ERR_TIMEOUT
     bool count_pairs = false;  // diagnostic pass: count the core test's distance evaluations
+    hpd_tuning tuning = {0, 0, 0};  // 0 fields: the size-class table, then the defaults
 };
+
+// Built-in tuning, and the table of hpd_set_tuning_table, resolved for one request.
+constexpr int kDefaultSparseQueries = 8;
+constexpr int kDefaultDenseMinPoints = 128;
+constexpr int kDefaultGreedyTiles = 6;
+hpd_tuning resolve_tuning(const hpd_tuning& own, int64_t n, int d);
+int set_tuning_table(const hpd_tuning_entry* entries, int32_t n_entries);
 
 struct RunInfo {
     int64_t n_cells = 0, n_core = 0, n_ambiguous = 0, tie_iterations = 0, core_pairs = 0;

@@ -1,4 +1,8 @@
 // Small shared kernels and the grow-only device arena.
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
 #include "hpd_internal.h"
 
 namespace hpd {
@@ -35,6 +39,40 @@ cudaError_t Arena::reserve(size_t bytes) {
     }
     cap = want;
     return cudaSuccess;
+}
+
+namespace {
+std::mutex g_tuning_mu;
+std::vector<hpd_tuning_entry> g_tuning_table;
+}  // namespace
+
+hpd_tuning resolve_tuning(const hpd_tuning& own, int64_t n, int d) {
+    hpd_tuning t = own;
+    {
+        std::lock_guard<std::mutex> lock(g_tuning_mu);
+        for (const auto& e : g_tuning_table) {
+            if (n <= e.max_points && (e.dims == 0 || e.dims == d)) {
+                if (!t.sparse_queries) t.sparse_queries = e.tuning.sparse_queries;
+                if (!t.dense_min_points) t.dense_min_points = e.tuning.dense_min_points;
+                if (!t.greedy_tiles) t.greedy_tiles = e.tuning.greedy_tiles;
+                break;
+            }
+        }
+    }
+    if (!t.sparse_queries) t.sparse_queries = kDefaultSparseQueries;
+    if (!t.dense_min_points) t.dense_min_points = kDefaultDenseMinPoints;
+    if (!t.greedy_tiles) t.greedy_tiles = kDefaultGreedyTiles;
+    t.sparse_queries = std::min(std::max(t.sparse_queries, 0), 32);
+    t.dense_min_points = std::max(t.dense_min_points, 32);
+    t.greedy_tiles = std::max(t.greedy_tiles, 1);
+    return t;
+}
+
+int set_tuning_table(const hpd_tuning_entry* entries, int32_t n_entries) {
+    if (n_entries < 0 || n_entries > 64 || (n_entries > 0 && !entries)) return HPD_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(g_tuning_mu);
+    g_tuning_table.assign(entries, entries + n_entries);
+    return HPD_OK;
 }
 
 Arena::~Arena() {

@@ -89,6 +89,8 @@ int hpd_cluster_device_noalloc(float epsilon, uint64_t min_points, int32_t cell_
     rq.d_labels = d_labels;
     rq.stream = static_cast<cudaStream_t>(stream);
     rq.no_dense = true;
+    // the built-in tuning, never the process-wide table: the scratch budget is sized for it
+    rq.tuning = hpd_tuning{kDefaultSparseQueries, kDefaultDenseMinPoints, kDefaultGreedyTiles};
     RunInfo info;
     std::string err;
     rc = dtype == HPD_F32 ? run_pipeline<float>(rq, small, main, nullptr, info, err)

@@ -89,7 +89,6 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
         }                                                                                                    \
     } while (0)
 
-constexpr int kDenseMinPoints = 128;  // cells with this many points take the dense-cell path
 constexpr int kFineMinPoints = 65536;  // a largest cell this big selects the finer sub-cell split
 constexpr int kJumpPasses = 3;          // relaxation passes followed by a pointer-jumping sweep
 
@@ -188,6 +187,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     const int d = rq.d;
     cudaStream_t s = rq.stream;
     const bool timed = tm && tm->ok;
+    const hpd_tuning tune = resolve_tuning(rq.tuning, rq.n, rq.d);
     int bits = 0;
     while (bits < 64 && ((g.total - 1) >> bits) != 0) ++bits;
 
@@ -226,7 +226,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         dense_groups *= std::max(dense_k, 1);
         groups_cap *= std::max(fine_k, 1);
     }
-    const int64_t dense_max = (int64_t)n / kDenseMinPoints + 1;
+    const int64_t dense_max = (int64_t)n / tune.dense_min_points + 1;
     need += 3 * (size_t)n * 4 + (size_t)dense_max * (3 * groups_cap + 2) * 4;  // dense-cell tables
     need += dense_k ? (size_t)dense_max * groups_cap * 2 * d * sizeof(T) : 0;   // sub-cell boxes
     need += dense_k ? (size_t)n * d * sizeof(T) : 0;                 // dense cells' coordinates by sub-cell
@@ -369,6 +369,8 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
     a.cellrank = rank;
     a.cell_rep = cell_rep;
     a.cell_flags = cell_flags;
+    a.sparse_queries = tune.sparse_queries;
+    a.greedy_tiles = tune.greedy_tiles;
     const int mode = rq.dist_mode;
     const unsigned qgrid = blocks_for(n_items, 4);
     const size_t qsmem = 4 * ((size_t)tile_stride(d) * 32 * sizeof(T) + 32 * sizeof(int));
@@ -381,7 +383,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         da.k = dense_k;
         da.groups = 1;
         for (int k = 0; k < d; ++k) da.groups *= dense_k;
-        da.min_points = kDenseMinPoints;
+        da.min_points = tune.dense_min_points;
         da.scale = (double)dense_k / (double)rq.eps;
         for (int k = 0; k < d; ++k) da.mins_d[k] = (double)mins[k];
         da.dense_id = dense_id;

@@ -206,6 +206,8 @@ struct QueryArgs {
     int* amb_out;         // undecided ambiguous borders after a decision round
     int* n_amb_out;
     unsigned long long* pair_count;  // diagnostic pass: distance evaluations of the core test
+    int sparse_queries;   // work items of at most this many points take the core test's flat path
+    int greedy_tiles;     // candidate tiles a work item of the greedy descent scans at most
     int4* chunks;         // tie-break chunk tasks (item, cell, first, end position) of a pass
     int* n_chunks;
     int chunk_cap;

@@ -485,8 +485,6 @@ static __global__ void k_tie_compact(uint32_t* item_flag, const uint32_t* pos, i
     }
 }
 
-constexpr int kGreedyTiles = 6;  // tiles a work item of the greedy descent scans at most
-
 // Greedy descent step: g(p) = some core eps-neighbour below p (p itself if none).
 // Any decreasing core edge leads to a position reachable from p, so following g
 // from p (pointer jumping) ends at an upper bound of L(p) - 1, equal to the
@@ -515,10 +513,10 @@ __device__ __forceinline__ void tie_greedy_item(const QueryArgs<T>& a, int item)
         if (found || !is_core || qi >= p) return;
         if (within<T, M, D>(a, q, tile, u)) { g = qi; found = true; }
     };
-    // the descent is a bound, not a result: a warp stops after kGreedyTiles tiles, and a
+    // the descent is a bound, not a result: a warp stops after a.greedy_tiles tiles, and a
     // lane without a hit by then keeps its own position (values only need to be reachable)
     int tiles = 0;
-    auto done = [&]() { return ++tiles >= kGreedyTiles || __all_sync(0xffffffffu, found); };
+    auto done = [&]() { return ++tiles >= a.greedy_tiles || __all_sync(0xffffffffu, found); };
     // lower positions of the own cell first (most pairs inside a cell are within eps),
     // then the lower face across the most significant dimension, then the rest
     bool all = scan_range(a, tile, a.ct.start[r], pend, aux_of, pair, done);

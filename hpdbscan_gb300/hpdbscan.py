@@ -62,6 +62,12 @@ class HPDBSCAN:
         """Relaxation passes of the exact tie-break before HPD_ERR_TIMEOUT; 0: default."""
         _lib.raise_for(self._lib.hpd_set_tie_pass_limit(self._h, int(passes)))
 
+    def set_tuning(self, sparse_queries: int = 0, dense_min_points: int = 0, greedy_tiles: int = 0) -> None:
+        """Work decomposition of this handle's calls (labels do not depend on it; 0: the
+        size-class table, then the built-in default)."""
+        t = _lib.Tuning(int(sparse_queries), int(dense_min_points), int(greedy_tiles))
+        _lib.raise_for(self._lib.hpd_set_tuning(self._h, ctypes.byref(t)))
+
     def set_diagnostics(self, flags: int = 0) -> None:
         """DIAG_COUNT_PAIRS: count the core test's distance evaluations (stats core_pairs)."""
         _lib.raise_for(self._lib.hpd_set_diagnostics(self._h, int(flags)))

@@ -37,9 +37,22 @@ def _job(points, eps, min_points, deadline_ms=0.0):
     return j, pts, labels
 
 
+_TABLE_LOADED = False
+
+
+def _load_tuning_table():
+    """Register the autotuner's size-class table (hpdbscan_gb300/tuning_table.json) once."""
+    global _TABLE_LOADED
+    if not _TABLE_LOADED:
+        from . import tune
+        tune.load_table()
+        _TABLE_LOADED = True
+
+
 def cluster_batch(items, workers: int = 8, with_stats: bool = False):
     """Labels of every (points, eps, min_points) item, clustered concurrently."""
     lib = _lib.load()
+    _load_tuning_table()
     built = [_job(*it) for it in items]
     arr = (_lib.Job * len(built))(*[b[0] for b in built])
     rc = lib.hpd_cluster_batch(arr, len(built), workers)
@@ -60,6 +73,7 @@ class Server:
     def __init__(self, workers: int = 8, budget_bytes: int = 120 << 30, reserve_points: int = 0,
                  reserve_dims: int = 3):
         self._lib = _lib.load()
+        _load_tuning_table()
         h = ctypes.c_void_p()
         rc = self._lib.hpd_server_create(workers, budget_bytes, reserve_points, reserve_dims, ctypes.byref(h))
         if rc:

@@ -116,6 +116,32 @@ int hpd_set_tie_pass_limit(hpd_handle* h, int32_t passes);
 typedef enum { HPD_DIAG_COUNT_PAIRS = 1 } hpd_diag;
 int hpd_set_diagnostics(hpd_handle* h, int32_t flags);
 
+/* Tuning of the engine's work decomposition (no counterpart in the reference; labels
+ * do not depend on it).  0 in a field keeps the built-in default.
+ *   sparse_queries    work items of at most this many points test their queries against
+ *                     one flat candidate list of the neighbour cells (default 8, max 32);
+ *   dense_min_points  cells with at least this many points are connected through
+ *                     certified sub-cells (default 128, min 32);
+ *   greedy_tiles      candidate tiles a work item of the tie-break's greedy descent
+ *                     scans at most (default 6). */
+typedef struct {
+    int32_t sparse_queries;
+    int32_t dense_min_points;
+    int32_t greedy_tiles;
+} hpd_tuning;
+int hpd_set_tuning(hpd_handle* h, const hpd_tuning* tuning);
+
+/* A process-wide table of tunings by size class, consulted by every call whose handle
+ * (or batch / served job) has no tuning of its own: the first entry with
+ * n <= max_points and d == dims applies (dims 0 matches any d).  Written by the
+ * autotuner (hpdbscan_gb300/tune.py); n_entries 0 clears it.  At most 64 entries. */
+typedef struct {
+    int64_t max_points;
+    int32_t dims;
+    hpd_tuning tuning;
+} hpd_tuning_entry;
+int hpd_set_tuning_table(const hpd_tuning_entry* entries, int32_t n_entries);
+
 /* Test hook (no counterpart in the reference) for the next call on the handle:
  * HPD_INJECT_FAIL_ALLOC makes the first device allocation the call needs fail without
  * being attempted, so the call returns HPD_ERR_NOMEM. */

@@ -57,3 +57,11 @@ def test_cluster_rejects_null_handle(engine_lib):
 
 def test_version_string(engine_lib):
     assert engine_lib.hpd_version().startswith(b"hpdbscan_gb300")
+
+
+def test_tuning_table_bounds(engine_lib):
+    from hpdbscan_gb300 import _lib
+    arr = (_lib.TuningEntry * 65)()
+    assert engine_lib.hpd_set_tuning_table(arr, 65) == 1
+    assert engine_lib.hpd_set_tuning_table(None, 1) == 1
+    assert engine_lib.hpd_set_tuning_table(None, 0) == 0
