@@ -10,7 +10,8 @@ and requires the identical label vector (same sha256); on a mismatch it reports 
 kind of point differs.
 
 Sets: the 10M-point 3-D benchmark workload (eps 0.005, minPoints 16) and the skewed
-2-D density at 1M points (eps 1e-3, minPoints 32).
+2-D density at 1M and 5M points (eps 1e-3, minPoints 32; the upstream single-thread
+run takes 312 s and 2.4 h on these).
 """
 import hashlib
 import os
@@ -69,4 +70,10 @@ def test_blobs10m_repeatable(blobs10m):
 def test_skewed1m_bit_exact(gpu):
     from hpdbscan_gb300 import HPDBSCAN, workloads
     w, z = _load("skewed1m_s0", lambda: workloads.skewed_2d(seed=0, n=1_000_000))
+    _check(HPDBSCAN(w.eps, w.min_points).cluster_array(w.points), z)
+
+
+def test_skewed5m_bit_exact(gpu):
+    from hpdbscan_gb300 import HPDBSCAN, workloads
+    w, z = _load("skewed5m_s0", lambda: workloads.skewed_2d(seed=0, n=5_000_000))
     _check(HPDBSCAN(w.eps, w.min_points).cluster_array(w.points), z)
