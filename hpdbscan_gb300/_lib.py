@@ -25,7 +25,8 @@ EXPORTS = ("hpd_create", "hpd_destroy", "hpd_set_arith", "hpd_set_tie_break", "h
            "hpd_set_diagnostics", "hpd_debug_inject", "hpd_cluster", "hpd_cluster_device",
            "hpd_get_stats", "hpd_last_error", "hpd_version", "hpd_cluster_device_noalloc",
            "hpd_noalloc_last_error", "hpd_cluster_batch", "hpd_server_create", "hpd_server_submit",
-           "hpd_server_poll", "hpd_server_wait", "hpd_server_destroy", "hpd_server_last_error")
+           "hpd_server_poll", "hpd_server_wait", "hpd_server_destroy", "hpd_server_last_error",
+           "hpd_h5_read", "hpd_h5_free", "hpd_h5_write")
 
 
 class Job(ctypes.Structure):
@@ -123,6 +124,14 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.hpd_server_destroy.restype = None
     lib.hpd_server_last_error.argtypes = []
     lib.hpd_server_last_error.restype = ctypes.c_char_p
+    lib.hpd_h5_read.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p),
+                                ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32),
+                                ctypes.POINTER(ctypes.c_int32)]
+    lib.hpd_h5_read.restype = ctypes.c_int
+    lib.hpd_h5_free.argtypes = [ctypes.c_void_p]
+    lib.hpd_h5_free.restype = None
+    lib.hpd_h5_write.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64]
+    lib.hpd_h5_write.restype = ctypes.c_int
     _lib = lib
     return lib
 

@@ -32,7 +32,9 @@ def nvcc() -> str:
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    """Every translation unit of the library: the CUDA sources and the host-only C++ ones."""
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
+                  if f.endswith(".cu") or (f.endswith(".cpp") and f != "hpdbscan_cli.cpp"))
 
 
 def _flags():
@@ -53,7 +55,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     srcs = sources()
-    objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
+    objs = [os.path.join(BUILD, os.path.splitext(os.path.basename(s))[0] + ".o") for s in srcs]
     jobs = []
     for s, o in zip(srcs, objs):
         if _stale(o, s) or ptxas_info:

@@ -100,6 +100,8 @@ void disarm_alloc_failure(hpd_handle* h) {
 }
 }  // namespace
 
+void hpd::set_last_error(const std::string& msg) { g_error = msg; }
+
 extern "C" {
 
 const char* hpd_last_error(void) { return g_error.c_str(); }

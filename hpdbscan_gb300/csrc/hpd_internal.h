@@ -10,6 +10,9 @@
 
 namespace hpd {
 
+// Sets the message of hpd_last_error() for this thread (the C ABI's error channel).
+void set_last_error(const std::string& msg);
+
 // ------------------------------------------------------------ scan / sort
 int64_t scan_scratch_elems(int64_t n);
 template <typename T>

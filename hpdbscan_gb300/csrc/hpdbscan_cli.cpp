@@ -9,9 +9,11 @@
 // include/spatial_index.h:548-602).  Like upstream, errors go to stderr and the exit
 // code is always 0.
 //
-// Files: libhdf5 is not available to this build, so datasets are NumPy .npy files
-// (2-D C-order array of one of the ten element types in; 1-D int64 labels out).  The
-// dataset-name flags are accepted; for .npy files the file is the dataset.
+// Files are HDF5 (read and written by the library's own implementation of the format,
+// hpd_h5_read / hpd_h5_write; the labels become a 1-D int64 dataset added to the
+// output file, which may be the input file, as upstream).  A file name ending in .npy
+// is a NumPy array instead (2-D C-order array in; 1-D int64 labels out) and the
+// dataset flag is ignored for it.
 #include <cctype>
 #include <chrono>
 #include <cstdint>
@@ -140,17 +142,33 @@ void write_npy(const std::string& path, const std::vector<int64_t>& labels) {
     if (!ok) throw std::runtime_error("Failed to write data, target data set is probably of wrong size or type");
 }
 
-bool is_hdf5(const std::string& path) {
-    const std::string lower = [&] {
-        std::string s = path;
-        for (auto& c : s) c = (char)std::tolower((unsigned char)c);
-        return s;
-    }();
-    auto ends = [&](const char* suf) {
-        const size_t n = std::strlen(suf);
-        return lower.size() >= n && lower.compare(lower.size() - n, n, suf) == 0;
-    };
-    return ends(".h5") || ends(".hdf5") || ends(".he5");
+bool is_npy(const std::string& path) {
+    return path.size() >= 4 && path.compare(path.size() - 4, 4, ".npy") == 0;
+}
+
+// The input as the reference reads it: HDF5 dataset (or .npy array), element type kept.
+Npy read_input(const std::string& path, const std::string& dataset) {
+    if (is_npy(path)) return read_npy(path);
+    void* buf = nullptr;
+    int64_t n = 0;
+    int32_t d = 0, dtype = 0;
+    const int rc = hpd_h5_read(path.c_str(), dataset.c_str(), &buf, &n, &d, &dtype);
+    if (rc == HPD_ERR_INVALID || rc == HPD_ERR_UNSUPPORTED) throw std::invalid_argument(hpd_last_error());
+    if (rc != HPD_OK) throw std::runtime_error(hpd_last_error());
+    Npy out;
+    out.dtype = dtype;
+    out.shape = {n, d};
+    const char* p = static_cast<const char*>(buf);
+    out.data.assign(p, p + (size_t)n * (size_t)d * dtype_size(dtype));
+    hpd_h5_free(buf);
+    return out;
+}
+
+void write_output(const std::string& path, const std::string& dataset, const std::vector<int64_t>& labels) {
+    if (is_npy(path)) return write_npy(path, labels);
+    const int rc = hpd_h5_write(path.c_str(), dataset.c_str(), labels.data(), (int64_t)labels.size());
+    if (rc == HPD_ERR_INVALID || rc == HPD_ERR_UNSUPPORTED) throw std::invalid_argument(hpd_last_error());
+    if (rc != HPD_OK) throw std::runtime_error(hpd_last_error());
 }
 
 void usage() {
@@ -164,7 +182,7 @@ void usage() {
               << "  -o, --output arg          output file (default: data.h5)\n"
               << "      --input-dataset arg   input dataset name (default: DATA)\n"
               << "      --output-dataset arg  output dataset name (default: CLUSTERS)\n"
-              << "\nFiles are NumPy .npy arrays (2-D points in, 1-D int64 labels out).\n";
+              << "\nFiles are HDF5; a name ending in .npy is a NumPy array (2-D points in, 1-D int64 labels out).\n";
 }
 
 }  // namespace
@@ -202,8 +220,6 @@ int main(int argc, char** argv) {
         std::cerr << "Could not parse command line:" << std::endl << e.what() << std::endl;
         return 0;
     }
-    (void)in_ds;
-    (void)out_ds;
     (void)threads;
 
     std::vector<int64_t> labels;
@@ -211,8 +227,7 @@ int main(int argc, char** argv) {
     const auto t0 = std::chrono::steady_clock::now();
     try {
         if (hpd_create(epsilon, min_points, &h) != HPD_OK) throw std::invalid_argument(hpd_last_error());
-        if (is_hdf5(input)) throw std::invalid_argument("Could not open " + input + " (HDF5 input needs libhdf5, which this build lacks; use .npy)");
-        Npy data = read_npy(input);
+        Npy data = read_input(input, in_ds);
         labels.resize((size_t)data.shape[0]);
         std::cout << std::fixed << std::setw(11) << std::setprecision(6) << std::setfill(' ');
         const int rc = hpd_cluster(h, data.data.data(), data.shape[0], (int32_t)data.shape[1], data.dtype, threads,
@@ -258,8 +273,7 @@ int main(int argc, char** argv) {
     }
     hpd_destroy(h);
     try {
-        if (is_hdf5(output)) throw std::invalid_argument("Could not open " + output + " (HDF5 output needs libhdf5, which this build lacks; use .npy)");
-        write_npy(output, labels);
+        write_output(output, out_ds, labels);
     } catch (const std::exception& e) {
         std::cerr << e.what() << std::endl;
     }

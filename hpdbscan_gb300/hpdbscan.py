@@ -14,11 +14,11 @@ array.
 from __future__ import annotations
 
 import ctypes
-import os
 
 import numpy as np
 
 from . import _lib
+from .hdf5 import read_hdf5
 
 _DTYPES = {
     np.dtype(np.float32): _lib.F32, np.dtype(np.float64): _lib.F64,
@@ -79,12 +79,13 @@ class HPDBSCAN:
     def cluster(self, data, dataset: str | None = None, threads: int | None = None):
         """cluster(ndarray) | cluster(path, dataset[, threads]) -> tuple of int."""
         if isinstance(data, (str, bytes)):
+            # HPDBSCAN::cluster(path, dataset[, threads]) (include/hpdbscan.h:300-356): the
+            # dataset in its own element type, dispatched like the reference
+            if dataset is None:
+                raise TypeError("cluster(path, dataset[, threads]) needs the dataset name")
             path = data if isinstance(data, str) else data.decode()
-            # as the C++ header's file overload: a missing file is std::invalid_argument
-            # ("Could not open"), an existing one std::runtime_error (no HDF5 reader here)
-            if not os.path.isfile(path):
-                raise ValueError("Could not open " + path)
-            raise RuntimeError("HDF5 input is not supported by this build")
+            arr = read_hdf5(path, dataset.decode() if isinstance(dataset, bytes) else dataset)
+            return tuple(self.cluster_array(arr).tolist())
         arr = np.ascontiguousarray(np.asarray(data, dtype=np.float64))
         return tuple(self.cluster_array(arr).tolist())
 

@@ -14,17 +14,16 @@
  * are accepted; `threads` is accepted and unused (the work runs on the current GPU).
  *
  * Header-only over the C ABI (hpdbscan_gb300.h); link with -lhpdbscan_gb300 -lcudart.
- * The upstream `cluster<T>(Dataset&, int)` overload is not provided: Dataset is the
- * upstream's HDF5-backed container.  The file overloads need HDF5 support, which this
- * build does not have: a missing file raises the upstream "Could not open <path>",
- * an existing one std::runtime_error.
+ * The file overloads read the HDF5 dataset with the library's own HDF5 reader
+ * (hpd_h5_read, no libhdf5) and dispatch on its element type as upstream; the
+ * upstream `cluster<T>(Dataset&, int)` overload is not provided (Dataset is the
+ * upstream's libhdf5-backed container).
  */
 #ifndef HPDBSCAN_GB300_CXX_H
 #define HPDBSCAN_GB300_CXX_H
 
 #include <cstddef>
 #include <cstdint>
-#include <cstdio>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -74,12 +73,15 @@ public:
     Clusters cluster(const std::string& path, const std::string& dataset) { return cluster(path, dataset, 0); }
 
     Clusters cluster(const std::string& path, const std::string& dataset, int threads) {
-        (void)dataset;
-        (void)threads;
-        std::FILE* f = std::fopen(path.c_str(), "rb");
-        if (!f) throw std::invalid_argument("Could not open " + path);
-        std::fclose(f);
-        throw std::runtime_error("HDF5 input is not supported by this build");
+        void* data = nullptr;
+        int64_t n = 0;
+        int32_t d = 0, dtype = 0;
+        hpdbscan_gb300_detail::raise(hpd_h5_read(path.c_str(), dataset.c_str(), &data, &n, &d, &dtype));
+        std::vector<int64_t> labels(static_cast<std::size_t>(n));
+        const int status = hpd_cluster(m_handle, data, n, d, dtype, threads, labels.data());
+        hpd_h5_free(data);
+        hpdbscan_gb300_detail::raise(status);
+        return Clusters(labels.begin(), labels.end());
     }
 
     template <typename T>

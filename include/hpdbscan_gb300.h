@@ -18,6 +18,9 @@
  *                               swig/hpdbscan.i:27-34
  *   hpd_cluster_device          the same computation on buffers already in device memory
  *                               (no upstream counterpart; the host entry point uses it)
+ *   hpd_h5_read / hpd_h5_write  IO::read_hdf5 / IO::write_hdf5 (include/io.h:35-197)
+ *                               with the element-type dispatch of HPDBSCAN::cluster(path,
+ *                               dataset, threads) (include/hpdbscan.h:300-356)
  *   hpd_last_error             the what() of the std::invalid_argument / runtime_error
  *                               the upstream class throws (hpdbscan.h:296,327,340,350,354)
  */
@@ -227,6 +230,32 @@ int hpd_cluster_device_noalloc(float epsilon, uint64_t min_points, int32_t cell_
                                const void* d_data, int64_t n, int32_t d, int32_t dtype, int64_t* d_labels,
                                void* stream);
 const char* hpd_noalloc_last_error(void);
+
+/* HDF5 files (the reference's IO::read_hdf5 / IO::write_hdf5, include/io.h:35-197),
+ * read and written by the library's own implementation of the HDF5 file format (no
+ * libhdf5): superblock versions 0-3, symbol-table and compact link groups, fixed-point
+ * and IEEE floating-point data of either byte order, compact / contiguous / chunked
+ * (unfiltered) storage.
+ *
+ * hpd_h5_read: the 2-D dataset `dataset` (a path of groups separated by '/') of the
+ * file `path`, row-major in its own element type, in a buffer the library allocates
+ * (release it with hpd_h5_free); *n rows (points), *d columns, *dtype the hpd_dtype of
+ * the reference's dispatch (include/hpdbscan.h:309-355).  Errors: HPD_ERR_INVALID
+ * "Could not open <path>" / "Could not open dataset <name>" / "Data in dataset <name>
+ * should be a matrix"; HPD_ERR_UNSUPPORTED "Unsupported signed integer precision" and
+ * the other element-type messages; HPD_ERR_RUNTIME "Failed to read data" (a broken
+ * file, or compressed storage, with the reason in parentheses).
+ *
+ * hpd_h5_write: n int64 labels as the dataset `dataset` of the file `path` like the
+ * reference: the file is created if it does not exist; a dataset of that name is
+ * created as 1-D int64, or an existing one receives the labels (its first n elements
+ * for a 1-D dataset, else all of exactly n elements; integer targets saturate,
+ * floating-point targets round).  Errors: HPD_ERR_INVALID "Could not open <path>" /
+ * "Could not open dataset <name>"; HPD_ERR_RUNTIME "Failed to write data, target data
+ * set is probably of wrong size or type". */
+int hpd_h5_read(const char* path, const char* dataset, void** data, int64_t* n, int32_t* d, int32_t* dtype);
+void hpd_h5_free(void* data);
+int hpd_h5_write(const char* path, const char* dataset, const int64_t* labels, int64_t n);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char* hpd_last_error(void);

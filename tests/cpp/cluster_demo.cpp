@@ -1,5 +1,6 @@
 // Test driver for include/hpdbscan.h, written the way an upstream user calls the
 // HPDBSCAN class:  cluster_demo <points.f32> <n> <d> <eps> <minPts> <labels.i64>
+//                  cluster_demo --h5 <file.h5> <dataset> <eps> <minPts> <labels.i64>
 //                  cluster_demo --bad-eps
 #include <cstdint>
 #include <cstdio>
@@ -20,6 +21,24 @@ int main(int argc, char** argv) {
             return 0;
         }
         return 1;
+    }
+    if (argc == 7 && std::string(argv[1]) == "--h5") {
+        HPDBSCAN h(static_cast<float>(std::atof(argv[4])), static_cast<size_t>(std::atol(argv[5])));
+        Clusters c;
+        try {
+            c = h.cluster(std::string(argv[2]), std::string(argv[3]));
+        } catch (const std::invalid_argument& e) {
+            std::cout << "invalid_argument: " << e.what() << std::endl;
+            return 0;
+        } catch (const std::runtime_error& e) {
+            std::cout << "runtime_error: " << e.what() << std::endl;
+            return 0;
+        }
+        std::FILE* o = std::fopen(argv[6], "wb");
+        std::vector<int64_t> out(c.begin(), c.end());
+        std::fwrite(out.data(), sizeof(int64_t), out.size(), o);
+        std::fclose(o);
+        return 0;
     }
     if (argc != 7) return 2;
     const int n = std::atoi(argv[2]), d = std::atoi(argv[3]);

@@ -48,9 +48,3 @@ def test_cli_clusters_npy_file(gpu, oracle, cli, tmp_path):
     assert int(summary["Clusters"]) == len(np.unique(np.abs(want[want != 0])))
     assert int(summary["Noise points"]) == int((want == 0).sum())
     assert int(summary["Core points"]) == int((want < 0).sum())
-
-
-@pytest.mark.gpu
-def test_cli_hdf5_path_reports_missing_support(gpu, cli, tmp_path):
-    r = subprocess.run([cli, "-i", str(tmp_path / "data.h5")], capture_output=True, text=True)
-    assert r.returncode == 0 and "Could not open" in r.stderr
