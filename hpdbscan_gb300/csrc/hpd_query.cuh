@@ -89,6 +89,31 @@ struct KeepAll {
     __device__ __forceinline__ bool operator()(int) const { return true; }
 };
 
+// Hands the cells of nr (-1: none) to fn in lane order, warp-uniformly; false once fn stops.
+template <class Fn>
+__device__ __forceinline__ bool deliver_cells(int nr, Fn& fn) {
+    unsigned mask = __ballot_sync(0xffffffffu, nr >= 0);
+    while (mask) {
+        const int src = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int cr = __shfl_sync(0xffffffffu, nr, src);
+        if (!fn(cr, false)) return false;
+    }
+    return true;
+}
+
+// First cell rank whose key is at least `key` (m if none).
+__device__ __forceinline__ int lower_cell(const CellTable& ct, unsigned long long key) {
+    int lo = 0, hi = ct.m;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (ct.key[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+constexpr int kStencilDirectDims = 5;  // up to 3^5 offsets: every offset is enumerated
+
 template <class Fn, class Keep = KeepAll>
 __device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct, int r, int sel, Fn&& fn,
                                               bool own_last = false, Keep keep = Keep()) {
@@ -97,39 +122,97 @@ __device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct
     const unsigned long long key = ct.key[r];
     unsigned long long coord[kMaxDims];
     for (int s = 0; s < g.d; ++s) coord[s] = ct.ccoord[(size_t)s * ct.pitch + r];
-    int S = 1;
-    for (int s = 0; s < g.d; ++s) S *= 3;
-    const int center = (S - 1) / 2;
-    for (int b = 0; b < S; b += 32) {
-        const int o = b + (int)lane;
-        int nr = -1;
-        if (o < S && o != center) {
-            int rest = o;
-            bool ok = true;
-            unsigned long long nk = key;
-            for (int s = 0; s < g.d; ++s) {
-                const int dig = rest % 3;
-                rest /= 3;
-                if (dig == 0) {
-                    if (coord[s] == 0) ok = false; else nk -= g.stride[s];
-                } else if (dig == 2) {
-                    if (coord[s] + 1 >= g.dims[g.swapped[s]]) ok = false; else nk += g.stride[s];
+    if (g.d <= kStencilDirectDims) {
+        int S = 1;
+        for (int s = 0; s < g.d; ++s) S *= 3;
+        const int center = (S - 1) / 2;
+        for (int b = 0; b < S; b += 32) {
+            const int o = b + (int)lane;
+            int nr = -1;
+            if (o < S && o != center) {
+                int rest = o;
+                bool ok = true;
+                unsigned long long nk = key;
+                for (int s = 0; s < g.d; ++s) {
+                    const int dig = rest % 3;
+                    rest /= 3;
+                    if (dig == 0) {
+                        if (coord[s] == 0) ok = false; else nk -= g.stride[s];
+                    } else if (dig == 2) {
+                        if (coord[s] + 1 >= g.dims[g.swapped[s]]) ok = false; else nk += g.stride[s];
+                    }
                 }
+                if (ok && (sel == 0 || (sel == 1 ? nk < key : nk > key))) {
+                    nr = (ct.dense && !in_range(ct.guard, (long long)nk, (long long)g.total, kGuardStencilKey))
+                             ? -1 : find_cell(ct, nk);
+                    if (nr >= 0 && !in_range(ct.guard, nr, ct.m, kGuardStencilCell)) nr = -1;
+                }
+                // the per-cell filter runs on all lanes at once, hiding its load latency
+                if (nr >= 0 && !keep(nr)) nr = -1;
             }
-            if (ok && (sel == 0 || (sel == 1 ? nk < key : nk > key))) {
-                nr = (ct.dense && !in_range(ct.guard, (long long)nk, (long long)g.total, kGuardStencilKey))
-                         ? -1 : find_cell(ct, nk);
-                if (nr >= 0 && !in_range(ct.guard, nr, ct.m, kGuardStencilCell)) nr = -1;
-            }
-            // the per-cell filter runs on all lanes at once, hiding its load latency
-            if (nr >= 0 && !keep(nr)) nr = -1;
+            if (!deliver_cells(nr, fn)) return;
         }
-        unsigned mask = __ballot_sync(0xffffffffu, nr >= 0);
-        while (mask) {
-            const int src = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const int cr = __shfl_sync(0xffffffffu, nr, src);
-            if (!fn(cr, false)) return;
+    } else {
+        // Many dimensions: 3^d offsets (43M at d = 16) would dwarf the occupied cells.
+        // The block's neighbours have keys within [key - reach_lo, key + reach_hi]
+        // (stride s exceeds the reach of all lower positions), so the visit takes the
+        // cheaper of (a) the offsets that stay inside the grid, looked up one by one,
+        // and (b) the occupied cells of that key range, tested coordinate by coordinate.
+        // Both hand out the same cells in the same ascending-key order.
+        long long valid = 1;
+        unsigned long long reach_lo = 0, reach_hi = 0;
+        for (int s = 0; s < g.d; ++s) {
+            const bool lo = coord[s] > 0, hi = coord[s] + 1 < g.dims[g.swapped[s]];
+            valid *= 1 + (int)lo + (int)hi;
+            if (lo) reach_lo += g.stride[s];
+            if (hi) reach_hi += g.stride[s];
+        }
+        const unsigned long long klo = sel == 2 ? key + 1 : key - reach_lo;
+        const unsigned long long khi = sel == 1 ? key - 1 : key + reach_hi;
+        const int first = (sel == 1 && reach_lo == 0) ? r : lower_cell(ct, klo);
+        const int last = (sel == 2 && reach_hi == 0) ? r : lower_cell(ct, khi + 1);  // one past the range
+        if ((long long)(last - first) <= valid) {
+            for (int b = first; b < last; b += 32) {
+                const int cr = b + (int)lane;
+                int nr = -1;
+                if (cr < last && cr != r) {
+                    bool ok = true;
+                    for (int s = 0; s < g.d && ok; ++s) {
+                        const unsigned long long c = ct.ccoord[(size_t)s * ct.pitch + cr];
+                        ok = c + 1 >= coord[s] && c <= coord[s] + 1;
+                    }
+                    if (ok) nr = cr;
+                }
+                if (nr >= 0 && !keep(nr)) nr = -1;
+                if (!deliver_cells(nr, fn)) return;
+            }
+        } else {
+            // mixed-radix enumeration of the in-grid offsets, dimension 0 fastest
+            for (long long b = 0; b < valid; b += 32) {
+                const long long o = b + (long long)lane;
+                int nr = -1;
+                if (o < valid) {
+                    long long rest = o;
+                    bool own = true;
+                    unsigned long long nk = key;
+                    for (int s = 0; s < g.d; ++s) {
+                        const bool lo = coord[s] > 0, hi = coord[s] + 1 < g.dims[g.swapped[s]];
+                        const int n_dig = 1 + (int)lo + (int)hi;
+                        const int dig = (int)(rest % n_dig) + (lo ? 0 : 1);  // 0: -1, 1: same, 2: +1
+                        rest /= n_dig;
+                        if (dig == 0) nk -= g.stride[s];
+                        if (dig == 2) nk += g.stride[s];
+                        own = own && dig == 1;
+                    }
+                    if (!own && (sel == 0 || (sel == 1 ? nk < key : nk > key))) {
+                        nr = (ct.dense && !in_range(ct.guard, (long long)nk, (long long)g.total, kGuardStencilKey))
+                                 ? -1 : find_cell(ct, nk);
+                        if (nr >= 0 && !in_range(ct.guard, nr, ct.m, kGuardStencilCell)) nr = -1;
+                    }
+                    if (nr >= 0 && !keep(nr)) nr = -1;
+                }
+                if (!deliver_cells(nr, fn)) return;
+            }
         }
     }
     if (own_last) fn(r, true);

@@ -30,6 +30,11 @@ Sets:
   big_cells_d{2,3}   compact blobs (sigma eps/20) in cells of up to ~70,000 points,
                      ringed by points at every distance: cells this full take the
                      box-pruned queries and the finer sub-cell split
+  hidim_d{6,12,16}   blob mixtures in 6, 12 and 16 dimensions (12 and 16 with 64-bit
+                     cell ids; the upstream build enumerates up to 3^d neighbour cells
+                     per cell and takes minutes on hidim_d16)
+
+    python tests/golden/make_golden.py [name-prefix ...]   # all fixtures, or those named
 """
 from __future__ import annotations
 
@@ -141,10 +146,43 @@ def dims_case(d: int, seed: int):
     return pts[rng.permutation(len(pts))], eps
 
 
+def hidim_case(d: int, seed: int):
+    """Six Gaussian blobs (two of them side by side), a shell of fringe points just
+    outside each blob (borders), points between the side-by-side pair and uniform noise,
+    in d dimensions; eps spans a quarter to a tenth of the unit extent, and for d = 16
+    the first dimension is twice as wide, so the grid has more than 2^32 cells."""
+    rng = np.random.default_rng(seed)
+    eps, sig, n_blob, n_noise, wide = {6: (0.08, 0.35, 3000, 2000, 1.0), 12: (0.1, 0.2, 500, 500, 1.0),
+                                       16: (0.25, 0.15, 400, 150, 2.0)}[d]
+    fringe = {6: (0.6, 1.1), 12: (0.3, 0.9), 16: (0.3, 0.9)}[d]
+    ext = np.ones(d)
+    ext[0] = wide
+    centres = rng.random((6, d)) * ext * 0.9 + 0.05
+    v = rng.standard_normal(d)
+    centres[1] = centres[0] + v / np.linalg.norm(v) * 2.2 * eps * np.sqrt(d) * sig
+    blobs = [c + rng.normal(0, eps * sig, (n_blob, d)) for c in centres]
+    radius = eps * sig * np.sqrt(d)
+    for c in centres:
+        u = rng.standard_normal((n_blob // 10, d))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        blobs.append(c + u * (radius + eps * rng.uniform(*fringe, (len(u), 1))))
+    blobs.append((centres[0] + centres[1]) / 2 + rng.normal(0, eps * 0.15, (40, d)))
+    pts = np.concatenate(blobs + [rng.random((n_noise, d)) * ext]).astype(np.float32)
+    return pts[rng.permutation(len(pts))], eps
+
+
 def main():
     if not po.ref_available():
         po.build(ref=True)
     os.makedirs(HERE, exist_ok=True)
+    only = sys.argv[1:]
+    if only:  # regenerate only the named fixtures
+        global save
+        keep_save = save
+
+        def save(name, *a, **k):  # noqa: F811
+            if any(name.startswith(o) for o in only):
+                keep_save(name, *a, **k)
     for s in (0, 1):
         w = wl.blobs_100k(seed=s)
         save(f"blobs100k_s{s}", w.points, w.eps, w.min_points, store_points=False, regen=f"blobs_100k:{s}")
@@ -191,6 +229,10 @@ def main():
     for d in (2, 3):
         pts, eps = big_cells(d, seed=60 + d)
         save(f"big_cells_d{d}", pts, eps, 40)
+    for d in (6, 12, 16):
+        if not only or any(f"hidim_d{d}".startswith(o) for o in only):
+            pts, eps = hidim_case(d, seed=80 + d)
+            save(f"hidim_d{d}", pts, eps, 8)
     manifest = {
         "reference_build": "upstream include/*.h via oracle/Makefile: g++ -std=c++11 -Ofast -fopenmp",
         "compiler": subprocess.run(["g++", "--version"], capture_output=True, text=True).stdout.splitlines()[0],

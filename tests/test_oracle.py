@@ -12,7 +12,13 @@ import pytest
 from conftest import golden_names, load_golden
 
 
-@pytest.mark.parametrize("name", golden_names())
+# The oracle walks every in-grid neighbour cell like the reference (up to 3^d per cell):
+# on hidim_d16 that takes about 15 minutes (it agreed with the upstream labels when the
+# fixture was made), too long for the CPU suite; the GPU tests check that fixture.
+SLOW_FOR_ORACLE = {"hidim_d16"}
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if n not in SLOW_FOR_ORACLE])
 def test_oracle_matches_golden(oracle, name):
     pts, eps, mp, labels = load_golden(name)
     got = oracle.cluster(pts, eps, mp, threads=1)
