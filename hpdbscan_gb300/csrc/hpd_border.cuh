@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(128) k_border(QueryArgs<T> a) {
         if (within<T, M, D>(a, q, tile, u)) hit(rep);
     };
     auto done = [&]() { return __all_sync(0xffffffffu, !active || multi); };
-    visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
+    visit_stencil<D>(a.g, a.ct, r, 0, [&](int cr, bool) {
         const int rep_c = a.cell_rep[cr];
         if (rep_c == kNoCore) return true;
         const bool dense = PRUNE && pruned_cell(a, cr);

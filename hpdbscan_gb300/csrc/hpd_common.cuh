@@ -100,7 +100,7 @@ __device__ __forceinline__ F fold_sq(const F* t, int d) {
         F off = sq_(t[0]);
 #pragma unroll
         for (int k = 1; k < (D > 0 ? D : kMaxDims); ++k) {
-            if (D == 0 && k >= n) break;
+            if (D <= 0 && k >= n) break;
             off = add_(off, sq_(t[k]));
         }
         return off;
@@ -108,7 +108,7 @@ __device__ __forceinline__ F fold_sq(const F* t, int d) {
         F off = sq_(t[0]);
 #pragma unroll
         for (int k = 1; k < (D > 0 ? D : kMaxDims); ++k) {
-            if (D == 0 && k >= n) break;
+            if (D <= 0 && k >= n) break;
             off = fma_(t[k], t[k], off);
         }
         return off;

@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
         // lane loads one candidate and tests every open query against it (a ballot
         // counts the hits per query), so a candidate is loaded once for the item
         int nr = 0;
-        visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
+        visit_stencil<D>(a.g, a.ct, r, 0, [&](int cr, bool) {
             if (lane_id() == 0) s_rng[w][nr] = make_int2(a.ct.start[cr], a.ct.start[cr + 1]);
             ++nr;
             return true;
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
                 const int j = s_rng[w][lo].x + (t - s_pre[w][lo]);
 #pragma unroll
                 for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-                    if (D == 0 && k >= a.g.d) break;
+                    if (D <= 0 && k >= a.g.d) break;
                     c[k] = a.coords[(size_t)k * a.n + j];
                 }
             }
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
                 T qq[D > 0 ? D : kMaxDims];
 #pragma unroll
                 for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-                    if (D == 0 && k >= a.g.d) break;
+                    if (D <= 0 && k >= a.g.d) break;
                     qq[k] = shfl_val(q[k], src);
                 }
                 const bool hit = valid && within_vals<T, M, D>(a, qq, c);
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(128) k_core(QueryArgs<T> a) {
         if (active && within<T, M, D>(a, q, tile, u)) ++count;
     };
     auto done = [&]() { return __all_sync(0xffffffffu, !active || count >= limit); };
-    visit_stencil(a.g, a.ct, r, 0, [&](int cr, bool) {
+    visit_stencil<D>(a.g, a.ct, r, 0, [&](int cr, bool) {
         if constexpr (PRUNE) {
             if (pruned_cell(a, cr)) {
                 // a sub-cell wholly within eps adds its population without a scan; only

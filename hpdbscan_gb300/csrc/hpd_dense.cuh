@@ -224,13 +224,13 @@ __global__ void __launch_bounds__(256) k_dense_link(QueryArgs<T> a, DenseArgs da
 // warp per dense cell: a cell with >= kPruneMinPoints points flags every cell of its
 // 3^d block (itself included) with kCellNearBig.  Every writer sets the same bit of a
 // byte whose other bit no longer changes, so the unsynchronised updates agree.
-template <typename T>
+template <typename T, int DS>
 __global__ void __launch_bounds__(128) k_mark_near_big(QueryArgs<T> a, DenseArgs da) {
     const int id = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (id >= *da.n_dense) return;
     const int c = da.cells[id];
     if (a.ct.start[c + 1] - a.ct.start[c] < kPruneMinPoints) return;
-    visit_stencil(a.g, a.ct, c, 0, [&](int cr, bool) {
+    visit_stencil<DS>(a.g, a.ct, c, 0, [&](int cr, bool) {
         if (lane_id() == 0) a.cell_flags[cr] |= kCellNearBig;
         return true;
     });
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(128) k_dense_pairs(QueryArgs<T> a, DenseArgs d
                     pa = da.sec[s0 + x];
 #pragma unroll
                     for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-                        if (D == 0 && k >= d) break;
+                        if (D <= 0 && k >= d) break;
                         qa[k] = a.coords[(size_t)k * a.n + pa];
                     }
                     if (!a.core[pa] || (da.boxes && box_class<T, D>(qa, box + (size_t)g2 * 2 * d, d, eps2) == kBoxFar))
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(128) k_dense_pairs(QueryArgs<T> a, DenseArgs d
                         pb = a.core[j] ? j : -1;
 #pragma unroll
                         for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-                            if (D == 0 && k >= d) break;
+                            if (D <= 0 && k >= d) break;
                             cb[k] = a.coords[(size_t)k * a.n + j];
                         }
                     }
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(128) k_dense_pairs(QueryArgs<T> a, DenseArgs d
                         T cu[D > 0 ? D : kMaxDims];
 #pragma unroll
                         for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-                            if (D == 0 && k >= d) break;
+                            if (D <= 0 && k >= d) break;
                             cu[k] = shfl_val(cb[k], u);
                         }
                         const unsigned hit = __ballot_sync(0xffffffffu, pa >= 0 && within_vals<T, M, D>(a, qa, cu));

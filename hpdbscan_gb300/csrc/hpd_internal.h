@@ -91,5 +91,7 @@ struct RunInfo {
 // Runs the whole pipeline for element type T.  Returns a Status and fills `err`.
 template <typename T>
 int run_pipeline(const Request& rq, Arena& small, Arena& main, Timers* timers, RunInfo& info, std::string& err);
+template <typename T, bool WIDE>
+int run_pipeline_dims(const Request& rq, Arena& small, Arena& main, Timers* timers, RunInfo& info, std::string& err);
 
 }  // namespace hpd

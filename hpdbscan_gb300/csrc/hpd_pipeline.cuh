@@ -40,7 +40,13 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
 // GCC x86-64 order equals the sequential order.
 #define HPD_QUERY_DISPATCH(KERNEL, T, mode, d, grid, block, smem, stream, ...)                                 \
     do {                                                                                                     \
-        if constexpr (!Elem<T>::kFloat) {                                                                    \
+        if constexpr (WIDE) {                                                                                \
+            if constexpr (!Elem<T>::kFloat) KERNEL<T, kDistSeq, -1><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, -1><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else if ((mode) == kDistSeq) KERNEL<T, kDistSeq, -1><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else if ((mode) == kDistGccArm) KERNEL<T, kDistGccArm, -1><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else KERNEL<T, kDistGccX86, -1><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+        } else if constexpr (!Elem<T>::kFloat) {                                                             \
             /* integer sums wrap, so every summation order gives the same result */                          \
             if ((d) == 2) KERNEL<T, kDistSeq, 2><<<grid, block, smem, stream>>>(__VA_ARGS__);                \
             else if ((d) == 3) KERNEL<T, kDistSeq, 3><<<grid, block, smem, stream>>>(__VA_ARGS__);           \
@@ -63,10 +69,17 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
         }                                                                                                    \
     } while (0)
 
-// Same, for kernels with a trailing bool template parameter B.
+// Same, for kernels with a trailing bool template parameter B.  (Both expect the
+// pipeline's WIDE template parameter in scope.)
 #define HPD_QUERY_DISPATCH_B(KERNEL, B, T, mode, d, grid, block, smem, stream, ...)                                 \
     do {                                                                                                     \
-        if constexpr (!Elem<T>::kFloat) {                                                                    \
+        if constexpr (WIDE) {                                                                                \
+            if constexpr (!Elem<T>::kFloat) KERNEL<T, kDistSeq, -1, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else if ((mode) == kDistSeqFma) KERNEL<T, kDistSeqFma, -1, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else if ((mode) == kDistSeq) KERNEL<T, kDistSeq, -1, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else if ((mode) == kDistGccArm) KERNEL<T, kDistGccArm, -1, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+            else KERNEL<T, kDistGccX86, -1, B><<<grid, block, smem, stream>>>(__VA_ARGS__); \
+        } else if constexpr (!Elem<T>::kFloat) {                                                             \
             /* integer sums wrap, so every summation order gives the same result */                          \
             if ((d) == 2) KERNEL<T, kDistSeq, 2, B><<<grid, block, smem, stream>>>(__VA_ARGS__);                \
             else if ((d) == 3) KERNEL<T, kDistSeq, 3, B><<<grid, block, smem, stream>>>(__VA_ARGS__);           \
@@ -92,12 +105,14 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
 constexpr int kFineMinPoints = 65536;  // a largest cell this big selects the finer sub-cell split
 constexpr int kJumpPasses = 3;          // relaxation passes followed by a pointer-jumping sweep
 
-template <typename T, typename K>
+template <typename T, typename K, bool WIDE>
 int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, std::string& err, const Grid& g,
                    const T* mins, bool dense_ok);
 
-template <typename T>
-int run_pipeline(const Request& rq, Arena& small, Arena& main, Timers* tm, RunInfo& info, std::string& err) {
+// WIDE: the grid has more than kStencilDirectDims dimensions; its query kernels are
+// compiled separately (dimension template -1), in their own translation units.
+template <typename T, bool WIDE>
+int run_pipeline_dims(const Request& rq, Arena& small, Arena& main, Timers* tm, RunInfo& info, std::string& err) {
     using F = typename Elem<T>::F;
     const int64_t n = rq.n;
     const int d = rq.d;
@@ -175,11 +190,11 @@ int run_pipeline(const Request& rq, Arena& small, Arena& main, Timers* tm, RunIn
     g.total = total;
     const bool dense_ok = !rq.no_dense && total <= (1ull << 31) && total <= std::max<unsigned long long>(1ull << 26, 8ull * (unsigned long long)n);
     if (total <= (1ull << 32))
-        return run_pipeline_k<T, uint32_t>(rq, main, tm, info, err, g, mins, dense_ok);
-    return run_pipeline_k<T, unsigned long long>(rq, main, tm, info, err, g, mins, dense_ok);
+        return run_pipeline_k<T, uint32_t, WIDE>(rq, main, tm, info, err, g, mins, dense_ok);
+    return run_pipeline_k<T, unsigned long long, WIDE>(rq, main, tm, info, err, g, mins, dense_ok);
 }
 
-template <typename T, typename K>
+template <typename T, typename K, bool WIDE>
 int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, std::string& err, const Grid& g,
                    const T* mins, bool dense_ok) {
     using F = typename Elem<T>::F;
@@ -403,7 +418,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         k_dense_assign<T><<<blocks_for(n, 256), 256, 0, s>>>(a, da);
         k_dense_offsets<T><<<blocks_for(dense_max, 4), 128, 0, s>>>(a, da);
         k_dense_scatter<T><<<blocks_for(n, 256), 256, 0, s>>>(a, da);
-        if (prune) k_mark_near_big<T><<<blocks_for(dense_max, 4), 128, 0, s>>>(a, da);
+        if (prune) k_mark_near_big<T, WIDE ? -1 : 0><<<blocks_for(dense_max, 4), 128, 0, s>>>(a, da);
         a.dense_id = dense_id;
         a.dense_grp = dense_grp;
         a.dense_gidx = dense_gidx;
@@ -587,7 +602,7 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
                 // and the edge passes alone reach the same (exact) fixpoint
                 if (pass <= kJumpPasses) k_tie_jump<T><<<blocks_for(n, 256), 256, 0, s>>>(a);
                 HPD_CU(cudaMemsetAsync(a.n_wlist_out, 0, sizeof(int), s));
-                k_tie_schedule<T><<<list_grid, 128, 0, s>>>(a);
+                HPD_QUERY_DISPATCH(k_tie_schedule, T, mode, d, list_grid, 128, 0, s, a);
                 info.launches += 3;
                 if (trace) {
                     unsigned long long tc[2];
@@ -663,6 +678,12 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         cudaEventElapsedTime(&ms, tm->ev[10], tm->ev[3]); info.rules_ms = ms;
     }
     return kOk;
+}
+
+template <typename T>
+int run_pipeline(const Request& rq, Arena& small, Arena& main, Timers* tm, RunInfo& info, std::string& err) {
+    return rq.d > kStencilDirectDims ? run_pipeline_dims<T, true>(rq, small, main, tm, info, err)
+                                     : run_pipeline_dims<T, false>(rq, small, main, tm, info, err);
 }
 
 }  // namespace hpd

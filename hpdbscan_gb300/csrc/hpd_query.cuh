@@ -89,19 +89,6 @@ struct KeepAll {
     __device__ __forceinline__ bool operator()(int) const { return true; }
 };
 
-// Hands the cells of nr (-1: none) to fn in lane order, warp-uniformly; false once fn stops.
-template <class Fn>
-__device__ __forceinline__ bool deliver_cells(int nr, Fn& fn) {
-    unsigned mask = __ballot_sync(0xffffffffu, nr >= 0);
-    while (mask) {
-        const int src = __ffs(mask) - 1;
-        mask &= mask - 1;
-        const int cr = __shfl_sync(0xffffffffu, nr, src);
-        if (!fn(cr, false)) return false;
-    }
-    return true;
-}
-
 // First cell rank whose key is at least `key` (m if none).
 __device__ __forceinline__ int lower_cell(const CellTable& ct, unsigned long long key) {
     int lo = 0, hi = ct.m;
@@ -114,105 +101,132 @@ __device__ __forceinline__ int lower_cell(const CellTable& ct, unsigned long lon
 
 constexpr int kStencilDirectDims = 5;  // up to 3^5 offsets: every offset is enumerated
 
-template <class Fn, class Keep = KeepAll>
+// The neighbour visit past kStencilDirectDims dimensions.  3^d offsets (43M at d =
+// 16) would dwarf the occupied cells.  The block's neighbours have keys within
+// [key - reach_lo, key + reach_hi] (stride s exceeds the reach of all lower
+// positions), so the visit walks the cheaper of (a) the offsets that stay inside the
+// grid, looked up one by one (mixed radix, dimension 0 fastest), and (b) the occupied
+// cells of that key range, tested coordinate by coordinate.  Both hand out the same
+// cells in the same ascending-key order as the direct enumeration.  wide_plan picks
+// the walk, wide_cell gives a lane its candidate.
+struct WidePlan {
+    long long count;  // steps of the walk
+    int first;        // range walk: first cell rank; -1: offset walk
+};
+
+__device__ __forceinline__ WidePlan wide_plan(const Grid& g, const CellTable& ct, int r, int sel) {
+    const unsigned long long key = ct.key[r];
+    long long valid = 1;
+    unsigned long long reach_lo = 0, reach_hi = 0;
+    for (int s = 0; s < g.d; ++s) {
+        const unsigned long long c = ct.ccoord[(size_t)s * ct.pitch + r];
+        const bool lo = c > 0, hi = c + 1 < g.dims[g.swapped[s]];
+        valid *= 1 + (int)lo + (int)hi;
+        if (lo) reach_lo += g.stride[s];
+        if (hi) reach_hi += g.stride[s];
+    }
+    const unsigned long long klo = sel == 2 ? key + 1 : key - reach_lo;
+    const unsigned long long khi = sel == 1 ? key - 1 : key + reach_hi;
+    const int first = (sel == 1 && reach_lo == 0) ? r : lower_cell(ct, klo);
+    const int last = (sel == 2 && reach_hi == 0) ? r : lower_cell(ct, khi + 1);  // one past the range
+    if ((long long)(last - first) <= valid) return WidePlan{last > first ? last - first : 0, first};
+    return WidePlan{valid, -1};
+}
+
+// Cell of step `step` of the walk (-1: not a neighbour, the own cell, or filtered by sel).
+__device__ __forceinline__ int wide_cell(const Grid& g, const CellTable& ct, int r, int sel, WidePlan plan,
+                                      long long step) {
+    if (step >= plan.count) return -1;
+    if (plan.first >= 0) {
+        const int cr = plan.first + (int)step;
+        if (cr == r) return -1;
+        for (int s = 0; s < g.d; ++s) {
+            const unsigned long long c = ct.ccoord[(size_t)s * ct.pitch + cr];
+            const unsigned long long o = ct.ccoord[(size_t)s * ct.pitch + r];
+            if (c + 1 < o || c > o + 1) return -1;
+        }
+        return cr;
+    }
+    const unsigned long long key = ct.key[r];
+    long long rest = step;
+    bool own = true;
+    unsigned long long nk = key;
+    for (int s = 0; s < g.d; ++s) {
+        const unsigned long long c = ct.ccoord[(size_t)s * ct.pitch + r];
+        const bool lo = c > 0, hi = c + 1 < g.dims[g.swapped[s]];
+        const int n_dig = 1 + (int)lo + (int)hi;
+        const int dig = (int)(rest % n_dig) + (lo ? 0 : 1);  // 0: -1, 1: same, 2: +1
+        rest /= n_dig;
+        if (dig == 0) nk -= g.stride[s];
+        if (dig == 2) nk += g.stride[s];
+        own = own && dig == 1;
+    }
+    if (own || (sel == 1 && nk >= key) || (sel == 2 && nk <= key)) return -1;
+    if (ct.dense && !in_range(ct.guard, (long long)nk, (long long)g.total, kGuardStencilKey)) return -1;
+    const int nr = find_cell(ct, nk);
+    return (nr >= 0 && in_range(ct.guard, nr, ct.m, kGuardStencilCell)) ? nr : -1;
+}
+
+// DS: the caller's compiled dimension count: 2 or 3, 0 for other counts up to
+// kStencilDirectDims (direct enumeration), -1 for counts past it (the wide walk; the
+// pipeline compiles its kernels separately for those).
+template <int DS = 0, class Fn, class Keep = KeepAll>
 __device__ __forceinline__ void visit_stencil(const Grid& g, const CellTable& ct, int r, int sel, Fn&& fn,
                                               bool own_last = false, Keep keep = Keep()) {
     if (!own_last && !fn(r, true)) return;
     const unsigned lane = lane_id();
+    if constexpr (DS < 0) {
+        const WidePlan plan = wide_plan(g, ct, r, sel);
+        for (long long b = 0; b < plan.count; b += 32) {
+            int nr = wide_cell(g, ct, r, sel, plan, b + (long long)lane);
+            if (nr >= 0 && !keep(nr)) nr = -1;
+            unsigned mask = __ballot_sync(0xffffffffu, nr >= 0);
+            while (mask) {
+                const int src = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int cr = __shfl_sync(0xffffffffu, nr, src);
+                if (!fn(cr, false)) return;
+            }
+        }
+        if (own_last) fn(r, true);
+        return;
+    }
     const unsigned long long key = ct.key[r];
     unsigned long long coord[kMaxDims];
     for (int s = 0; s < g.d; ++s) coord[s] = ct.ccoord[(size_t)s * ct.pitch + r];
-    if (g.d <= kStencilDirectDims) {
-        int S = 1;
-        for (int s = 0; s < g.d; ++s) S *= 3;
-        const int center = (S - 1) / 2;
-        for (int b = 0; b < S; b += 32) {
-            const int o = b + (int)lane;
-            int nr = -1;
-            if (o < S && o != center) {
-                int rest = o;
-                bool ok = true;
-                unsigned long long nk = key;
-                for (int s = 0; s < g.d; ++s) {
-                    const int dig = rest % 3;
-                    rest /= 3;
-                    if (dig == 0) {
-                        if (coord[s] == 0) ok = false; else nk -= g.stride[s];
-                    } else if (dig == 2) {
-                        if (coord[s] + 1 >= g.dims[g.swapped[s]]) ok = false; else nk += g.stride[s];
-                    }
+    int S = 1;
+    for (int s = 0; s < g.d; ++s) S *= 3;
+    const int center = (S - 1) / 2;
+    for (int b = 0; b < S; b += 32) {
+        const int o = b + (int)lane;
+        int nr = -1;
+        if (o < S && o != center) {
+            int rest = o;
+            bool ok = true;
+            unsigned long long nk = key;
+            for (int s = 0; s < g.d; ++s) {
+                const int dig = rest % 3;
+                rest /= 3;
+                if (dig == 0) {
+                    if (coord[s] == 0) ok = false; else nk -= g.stride[s];
+                } else if (dig == 2) {
+                    if (coord[s] + 1 >= g.dims[g.swapped[s]]) ok = false; else nk += g.stride[s];
                 }
-                if (ok && (sel == 0 || (sel == 1 ? nk < key : nk > key))) {
-                    nr = (ct.dense && !in_range(ct.guard, (long long)nk, (long long)g.total, kGuardStencilKey))
-                             ? -1 : find_cell(ct, nk);
-                    if (nr >= 0 && !in_range(ct.guard, nr, ct.m, kGuardStencilCell)) nr = -1;
-                }
-                // the per-cell filter runs on all lanes at once, hiding its load latency
-                if (nr >= 0 && !keep(nr)) nr = -1;
             }
-            if (!deliver_cells(nr, fn)) return;
+            if (ok && (sel == 0 || (sel == 1 ? nk < key : nk > key))) {
+                nr = (ct.dense && !in_range(ct.guard, (long long)nk, (long long)g.total, kGuardStencilKey))
+                         ? -1 : find_cell(ct, nk);
+                if (nr >= 0 && !in_range(ct.guard, nr, ct.m, kGuardStencilCell)) nr = -1;
+            }
+            // the per-cell filter runs on all lanes at once, hiding its load latency
+            if (nr >= 0 && !keep(nr)) nr = -1;
         }
-    } else {
-        // Many dimensions: 3^d offsets (43M at d = 16) would dwarf the occupied cells.
-        // The block's neighbours have keys within [key - reach_lo, key + reach_hi]
-        // (stride s exceeds the reach of all lower positions), so the visit takes the
-        // cheaper of (a) the offsets that stay inside the grid, looked up one by one,
-        // and (b) the occupied cells of that key range, tested coordinate by coordinate.
-        // Both hand out the same cells in the same ascending-key order.
-        long long valid = 1;
-        unsigned long long reach_lo = 0, reach_hi = 0;
-        for (int s = 0; s < g.d; ++s) {
-            const bool lo = coord[s] > 0, hi = coord[s] + 1 < g.dims[g.swapped[s]];
-            valid *= 1 + (int)lo + (int)hi;
-            if (lo) reach_lo += g.stride[s];
-            if (hi) reach_hi += g.stride[s];
-        }
-        const unsigned long long klo = sel == 2 ? key + 1 : key - reach_lo;
-        const unsigned long long khi = sel == 1 ? key - 1 : key + reach_hi;
-        const int first = (sel == 1 && reach_lo == 0) ? r : lower_cell(ct, klo);
-        const int last = (sel == 2 && reach_hi == 0) ? r : lower_cell(ct, khi + 1);  // one past the range
-        if ((long long)(last - first) <= valid) {
-            for (int b = first; b < last; b += 32) {
-                const int cr = b + (int)lane;
-                int nr = -1;
-                if (cr < last && cr != r) {
-                    bool ok = true;
-                    for (int s = 0; s < g.d && ok; ++s) {
-                        const unsigned long long c = ct.ccoord[(size_t)s * ct.pitch + cr];
-                        ok = c + 1 >= coord[s] && c <= coord[s] + 1;
-                    }
-                    if (ok) nr = cr;
-                }
-                if (nr >= 0 && !keep(nr)) nr = -1;
-                if (!deliver_cells(nr, fn)) return;
-            }
-        } else {
-            // mixed-radix enumeration of the in-grid offsets, dimension 0 fastest
-            for (long long b = 0; b < valid; b += 32) {
-                const long long o = b + (long long)lane;
-                int nr = -1;
-                if (o < valid) {
-                    long long rest = o;
-                    bool own = true;
-                    unsigned long long nk = key;
-                    for (int s = 0; s < g.d; ++s) {
-                        const bool lo = coord[s] > 0, hi = coord[s] + 1 < g.dims[g.swapped[s]];
-                        const int n_dig = 1 + (int)lo + (int)hi;
-                        const int dig = (int)(rest % n_dig) + (lo ? 0 : 1);  // 0: -1, 1: same, 2: +1
-                        rest /= n_dig;
-                        if (dig == 0) nk -= g.stride[s];
-                        if (dig == 2) nk += g.stride[s];
-                        own = own && dig == 1;
-                    }
-                    if (!own && (sel == 0 || (sel == 1 ? nk < key : nk > key))) {
-                        nr = (ct.dense && !in_range(ct.guard, (long long)nk, (long long)g.total, kGuardStencilKey))
-                                 ? -1 : find_cell(ct, nk);
-                        if (nr >= 0 && !in_range(ct.guard, nr, ct.m, kGuardStencilCell)) nr = -1;
-                    }
-                    if (nr >= 0 && !keep(nr)) nr = -1;
-                }
-                if (!deliver_cells(nr, fn)) return;
-            }
+        unsigned mask = __ballot_sync(0xffffffffu, nr >= 0);
+        while (mask) {
+            const int src = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int cr = __shfl_sync(0xffffffffu, nr, src);
+            if (!fn(cr, false)) return;
         }
     }
     if (own_last) fn(r, true);
@@ -370,7 +384,7 @@ __device__ __forceinline__ int box_class(const T* q, const T* box, int d, BoxRea
     R lo2 = 0, hi2 = 0;
 #pragma unroll
     for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-        if (D == 0 && k >= d) break;
+        if (D <= 0 && k >= d) break;
         const R lo = (R)box[k], hi = (R)box[d + k], x = (R)q[k];
         const R dn = x < lo ? lo - x : (x > hi ? x - hi : R(0));
         const R df = x - lo > hi - x ? x - lo : hi - x;
@@ -476,7 +490,7 @@ __device__ __forceinline__ void tile_load(const Tile<T>& tile, int u, int d, T* 
         const int S = tile_stride(d);
 #pragma unroll
         for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-            if (D == 0 && k >= d) break;
+            if (D <= 0 && k >= d) break;
             c[k] = tile.c[u * S + k];
         }
     } else if (D == 2) {
@@ -511,7 +525,7 @@ __device__ __forceinline__ bool int_within(const T* p, const T* q, int d, T eps2
     unsigned long long acc = 0;
 #pragma unroll
     for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-        if (D == 0 && k >= d) break;
+        if (D <= 0 && k >= d) break;
         const T t = (T)((unsigned long long)p[k] - (unsigned long long)q[k]);
         const unsigned long long w = (unsigned long long)(long long)t;
         acc += w * w;
@@ -528,7 +542,7 @@ __device__ __forceinline__ bool within_vals(const QueryArgs<T>& a, const T* q, c
         T t[D > 0 ? D : kMaxDims];
 #pragma unroll
         for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-            if (D == 0 && k >= a.g.d) break;
+            if (D <= 0 && k >= a.g.d) break;
             t[k] = sub_(q[k], c[k]);
         }
         return fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
@@ -546,7 +560,7 @@ __device__ __forceinline__ bool within(const QueryArgs<T>& a, const T* q, const 
         T t[D > 0 ? D : kMaxDims];
 #pragma unroll
         for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-            if (D == 0 && k >= a.g.d) break;
+            if (D <= 0 && k >= a.g.d) break;
             t[k] = sub_(q[k], c[k]);
         }
         return fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
@@ -557,7 +571,7 @@ template <typename T, int D>
 __device__ __forceinline__ void load_query(const QueryArgs<T>& a, int p, bool active, T* q) {
 #pragma unroll
     for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-        if (D == 0 && k >= a.g.d) break;
+        if (D <= 0 && k >= a.g.d) break;
         q[k] = active ? a.coords[(size_t)k * a.n + p] : T(0);
     }
 }

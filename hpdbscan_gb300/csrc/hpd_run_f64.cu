@@ -3,5 +3,8 @@
 #include "hpd_pipeline.cuh"
 
 namespace hpd {
+// grids past five dimensions: hpd_run_f64_wide.cu
+extern template int run_pipeline_dims<double, true>(const Request&, Arena&, Arena&, Timers*, RunInfo&, std::string&);
+template int run_pipeline_dims<double, false>(const Request&, Arena&, Arena&, Timers*, RunInfo&, std::string&);
 template int run_pipeline<double>(const Request&, Arena&, Arena&, Timers*, RunInfo&, std::string&);
 }

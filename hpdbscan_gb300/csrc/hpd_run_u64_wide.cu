@@ -1,0 +1,7 @@
+// Pipeline instantiation for uint64_t points on grids of more than five dimensions
+// (compiled apart from hpd_run_u64.cu to keep each translation unit short).
+#include "hpd_pipeline.cuh"
+
+namespace hpd {
+template int run_pipeline_dims<uint64_t, true>(const Request&, Arena&, Arena&, Timers*, RunInfo&, std::string&);
+}

@@ -2,5 +2,8 @@
 #include "hpd_pipeline.cuh"
 
 namespace hpd {
+// grids past five dimensions: hpd_run_u8_wide.cu
+extern template int run_pipeline_dims<uint8_t, true>(const Request&, Arena&, Arena&, Timers*, RunInfo&, std::string&);
+template int run_pipeline_dims<uint8_t, false>(const Request&, Arena&, Arena&, Timers*, RunInfo&, std::string&);
 template int run_pipeline<uint8_t>(const Request&, Arena&, Arena&, Timers*, RunInfo&, std::string&);
 }

@@ -24,7 +24,7 @@ __device__ __forceinline__ void scan_point(const QueryArgs<T>& a, int p, Hit&& h
     T q[D > 0 ? D : kMaxDims];
 #pragma unroll
     for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-        if (D == 0 && k >= a.g.d) break;
+        if (D <= 0 && k >= a.g.d) break;
         q[k] = a.coords[(size_t)k * a.n + p];
     }
     // the cell of p: binary search on cell starts
@@ -33,14 +33,14 @@ __device__ __forceinline__ void scan_point(const QueryArgs<T>& a, int p, Hit&& h
         int mid = (lo + hi) >> 1;
         if (a.ct.start[mid] <= p) lo = mid; else hi = mid;
     }
-    visit_stencil(a.g, a.ct, lo, 0, [&](int cr, bool) {
+    visit_stencil<D>(a.g, a.ct, lo, 0, [&](int cr, bool) {
         const int ce = a.ct.start[cr + 1];
         for (int j = a.ct.start[cr] + (int)lane; j < ce; j += 32) {
             if (!a.core[j]) continue;
             T c[D > 0 ? D : kMaxDims];
 #pragma unroll
             for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-                if (D == 0 && k >= a.g.d) break;
+                if (D <= 0 && k >= a.g.d) break;
                 c[k] = a.coords[(size_t)k * a.n + j];
             }
             bool in;
@@ -50,7 +50,7 @@ __device__ __forceinline__ void scan_point(const QueryArgs<T>& a, int p, Hit&& h
                 T t[D > 0 ? D : kMaxDims];
 #pragma unroll
                 for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-                    if (D == 0 && k >= a.g.d) break;
+                    if (D <= 0 && k >= a.g.d) break;
                     t[k] = sub_(q[k], c[k]);
                 }
                 in = fold_sq<T, M, D>(t, a.g.d) <= a.eps2;
@@ -252,7 +252,7 @@ __device__ __forceinline__ void tie_edge_item(const QueryArgs<T>& a, int item) {
     int worst0 = active ? myl : INT_MIN;  // largest lane value at the start: a cell must beat it
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) worst0 = max(worst0, __shfl_xor_sync(0xffffffffu, worst0, o));
-    visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
+    visit_stencil<D>(a.g, a.ct, r, 1, [&](int cr, bool own) {
         if (own) {
             // own cell: the lower chunks once, then the warp's own chunk: every lane
             // offers its value to the higher lanes of the chunk within eps; taking the
@@ -428,7 +428,7 @@ __global__ void k_tie_cell_min(QueryArgs<T> a) {
 
 // Next pass's work: the items of every cell whose lower stencil or own cell was
 // dirtied in this pass are appended to the next work list (warp per dirty cell).
-template <typename T>
+template <typename T, int M, int D>
 __global__ void __launch_bounds__(128) k_tie_schedule(QueryArgs<T> a) {
     const int nw = gridDim.x * 4;
     int cnt = *a.n_dlist;
@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(128) k_tie_schedule(QueryArgs<T> a) {
             if ((a.cell_flags[cr] & kCellUniform) && tmax_of(a, rep_c) < a.ct.start[cr]) return false;
             return atomicMax(a.sched_gen + cr, a.gen) < a.gen;
         };
-        visit_stencil(a.g, a.ct, c, 2, [&](int cr, bool own) {
+        visit_stencil<D>(a.g, a.ct, c, 2, [&](int cr, bool own) {
             if (own) {  // the stencil filter (claim, one neighbour per lane) skips the own cell
                 int fresh = 0;
                 if (lane == 0) fresh = claim(cr);
@@ -527,7 +527,7 @@ __device__ __forceinline__ void tie_greedy_item(const QueryArgs<T>& a, int item)
     if (face >= 0 && a.cell_rep[face] != kNoCore)
         all = scan_range(a, tile, a.ct.start[face], a.ct.start[face + 1], aux_of, pair, done);
     if (!all) {
-        visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
+        visit_stencil<D>(a.g, a.ct, r, 1, [&](int cr, bool own) {
             if (own || cr == face || a.cell_rep[cr] == kNoCore) return true;
             return !scan_range(a, tile, a.ct.start[cr], a.ct.start[cr + 1], aux_of, pair, done);
         });

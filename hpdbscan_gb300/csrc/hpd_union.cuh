@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(128) k_union_cross(QueryArgs<T> a) {
     };
     (void)rep_r;
     // pairs of single-component cells are joined by k_union_cells
-    visit_stencil(a.g, a.ct, r, 1, [&](int cr, bool own) {
+    visit_stencil<D>(a.g, a.ct, r, 1, [&](int cr, bool own) {
         if (own) return true;
         auto never = []() { return false; };
         scan_range_hits(a, tile, a.ct.start[cr], a.ct.start[cr + 1], test, aux_of, on_hit, never);
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(128) k_union_cells(QueryArgs<T> a) {
     const unsigned lane = lane_id();
     const int d = a.g.d;
     const int cs = a.ct.start[c], ce = a.ct.start[c + 1];
-    visit_stencil(a.g, a.ct, c, 1, [&](int cr, bool own) {
+    visit_stencil<D>(a.g, a.ct, c, 1, [&](int cr, bool own) {
         if (own) return true;
         const int rep_n = a.cell_rep[cr];
         if (same_component(a.parent, rep_c, rep_n)) return true;  // joined since the filter ran
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(128) k_union_cells(QueryArgs<T> a) {
                     T cu[D > 0 ? D : kMaxDims];
 #pragma unroll
                     for (int k = 0; k < (D > 0 ? D : kMaxDims); ++k) {
-                        if (D == 0 && k >= d) break;
+                        if (D <= 0 && k >= d) break;
                         cu[k] = shfl_val(vb[k], u);
                     }
                     const unsigned hit = __ballot_sync(0xffffffffu, ca && within_vals<T, M, D>(a, qa, cu));
