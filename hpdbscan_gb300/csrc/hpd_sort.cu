@@ -119,56 +119,92 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_upsweep(const K* __restr
 // 32 consecutive items; ranks within a round come from __match_any_sync, ranks
 // across rounds from per-warp digit counters, ranks across warps from a prefix
 // over the warps' counters.  Item order within each digit is therefore preserved.
+// Each item keeps only its packed (digit, rank); the block then lists its items in
+// digit order in shared memory and writes them out in that order, so that the items
+// of one digit go to consecutive addresses (coalesced runs) instead of one scattered
+// store per item.
 template <typename K>
 __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(const K* __restrict__ keys_in, const int32_t* __restrict__ vals_in,
                                                                   K* __restrict__ keys_out, int32_t* __restrict__ vals_out, int64_t n,
                                                                   int shift, const uint32_t* __restrict__ offsets, int nb) {
     __shared__ uint32_t wcnt[kSortWarps][kRadix];
-    __shared__ uint32_t s_off[kRadix];
+    __shared__ uint32_t s_off[kRadix];    // global start of each digit for this tile
+    __shared__ uint32_t s_start[kRadix];  // tile-local start of each digit
+    __shared__ uint16_t s_item[kSortTile];  // tile-local item of each tile-local position
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_total;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) (&wcnt[0][0])[i] = 0;
     s_off[threadIdx.x] = offsets[(int64_t)threadIdx.x * nb + blockIdx.x];
     __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * kSortTile + (int64_t)warp * (kSortItems * 32);
+    const int64_t tile0 = (int64_t)blockIdx.x * kSortTile;
+    const int wbase = warp * (kSortItems * 32);
     const unsigned lt_mask = (1u << lane) - 1u;
-    K k[kSortItems];
-    int32_t v[kSortItems];
-    uint32_t r[kSortItems];
+    uint32_t dr[kSortItems];  // digit << 16 | rank within the warp's items of that digit
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
-        const int64_t idx = base + i * 32 + lane;
+        const int64_t idx = tile0 + wbase + i * 32 + lane;
         const bool ok = idx < n;
-        k[i] = ok ? keys_in[idx] : K(0);
-        v[i] = ok ? vals_in[idx] : 0;
-        const uint32_t dig = ok ? ((uint32_t)(k[i] >> shift) & (kRadix - 1)) : 0x10000u + lane;
+        const uint32_t dig = ok ? ((uint32_t)(keys_in[idx] >> shift) & (kRadix - 1)) : 0x10000u + lane;
         const unsigned peers = __match_any_sync(0xffffffffu, dig);
         uint32_t before = 0;
         if (ok) before = wcnt[warp][dig];
         __syncwarp();
         if (ok && (31 - __clz(peers)) == lane) wcnt[warp][dig] = before + __popc(peers);
         __syncwarp();
-        r[i] = before + __popc(peers & lt_mask);
+        dr[i] = ok ? (dig << 16) | (before + __popc(peers & lt_mask)) : 0xffffffffu;
     }
     __syncthreads();
     {
+        // per digit (one per thread): the warps' counts become offsets within the
+        // digit, and the digit's tile-local start is the prefix over the digits
         uint32_t run = 0;
 #pragma unroll
         for (int w = 0; w < kSortWarps; ++w) {
-            uint32_t c = wcnt[w][threadIdx.x];
+            const uint32_t c = wcnt[w][threadIdx.x];
             wcnt[w][threadIdx.x] = run;
             run += c;
         }
+        const int dlane = threadIdx.x & 31, dwarp = threadIdx.x >> 5;
+        uint32_t inc = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (dlane >= o) inc += y;
+        }
+        if (dlane == 31) s_warp[dwarp] = inc;
+        __syncthreads();
+        if (dwarp == 0) {
+            const uint32_t wv = dlane < kSortWarps ? s_warp[dlane] : 0u;
+            uint32_t wi = wv;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+                if (dlane >= o) wi += y;
+            }
+            if (dlane < kSortWarps) s_warp[dlane] = wi - wv;
+            if (dlane == 31) s_total = wi;
+        }
+        __syncthreads();
+        s_start[threadIdx.x] = s_warp[dwarp] + inc - run;
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < kSortItems; ++i) {
-        const int64_t idx = base + i * 32 + lane;
-        if (idx < n) {
-            const uint32_t dig = (uint32_t)(k[i] >> shift) & (kRadix - 1);
-            const int64_t pos = (int64_t)s_off[dig] + wcnt[warp][dig] + r[i];
-            keys_out[pos] = k[i];
-            vals_out[pos] = v[i];
-        }
+        if (dr[i] == 0xffffffffu) continue;
+        const uint32_t dig = dr[i] >> 16;
+        const uint32_t lp = s_start[dig] + wcnt[warp][dig] + (dr[i] & 0xffffu);
+        s_item[lp] = (uint16_t)(wbase + i * 32 + lane);
+    }
+    __syncthreads();
+    const int cnt = (int)s_total;
+    for (int j = threadIdx.x; j < cnt; j += kSortThreads) {
+        const int64_t src = tile0 + s_item[j];
+        const K key = keys_in[src];
+        const uint32_t dig = (uint32_t)(key >> shift) & (kRadix - 1);
+        const int64_t pos = (int64_t)s_off[dig] + (j - (int)s_start[dig]);
+        keys_out[pos] = key;
+        vals_out[pos] = vals_in[src];
     }
 }
 
