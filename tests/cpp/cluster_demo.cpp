@@ -1,6 +1,8 @@
 // Test driver for include/hpdbscan.h, written the way an upstream user calls the
 // HPDBSCAN class:  cluster_demo <points.f32> <n> <d> <eps> <minPts> <labels.i64>
 //                  cluster_demo --h5 <file.h5> <dataset> <eps> <minPts> <labels.i64>
+//                  cluster_demo --io-roundtrip <in.h5> <dataset> <out.h5>
+//                  cluster_demo --io-cluster <in.h5> <dataset> <eps> <minPts> <out.h5>
 //                  cluster_demo --bad-eps
 #include <cstdint>
 #include <cstdio>
@@ -21,6 +23,31 @@ int main(int argc, char** argv) {
             return 0;
         }
         return 1;
+    }
+    if (argc == 5 && std::string(argv[1]) == "--io-roundtrip") {
+        // IO::read_hdf5 -> Dataset, then labels derived from the shape through IO::write_hdf5
+        try {
+            Dataset ds = IO::read_hdf5(argv[2], argv[3]);
+            std::cout << "shape " << ds.m_shape[0] << " " << ds.m_shape[1] << " type " << ds.m_type << std::endl;
+            Clusters c(static_cast<std::size_t>(ds.m_chunk[0]));
+            for (std::size_t i = 0; i < c.size(); ++i) c[i] = static_cast<Cluster>(i % 7) - 3;
+            IO::write_hdf5(argv[4], "CLUSTERS", c);
+        } catch (const std::invalid_argument& e) {
+            std::cout << "invalid_argument: " << e.what() << std::endl;
+        }
+        return 0;
+    }
+    if (argc == 7 && std::string(argv[1]) == "--io-cluster") {
+        HPDBSCAN h(static_cast<float>(std::atof(argv[4])), static_cast<size_t>(std::atol(argv[5])));
+        Dataset ds = IO::read_hdf5(argv[2], argv[3]);
+        Clusters c = h.cluster<float>(ds, 0);
+        IO::write_hdf5(argv[6], "CLUSTERS", c);
+        try {
+            h.cluster<double>(ds);
+        } catch (const std::invalid_argument& e) {
+            std::cout << "invalid_argument: " << e.what() << std::endl;
+        }
+        return 0;
     }
     if (argc == 7 && std::string(argv[1]) == "--h5") {
         HPDBSCAN h(static_cast<float>(std::atof(argv[4])), static_cast<size_t>(std::atol(argv[5])));
