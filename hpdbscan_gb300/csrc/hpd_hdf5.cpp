@@ -26,9 +26,7 @@
 #include <unistd.h>
 
 #include <algorithm>
-#include <cmath>
 #include <cstdint>
-#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <limits>
@@ -950,6 +948,18 @@ void write_into(File& f, const Dataset& ds, const int64_t* labels, uint64_t n) {
     throw Unsupported("writing chunked datasets");
 }
 
+// pwrite of the whole range (regular files may still return short counts).
+bool write_at(int fd, const unsigned char* p, uint64_t n, uint64_t at) {
+    while (n > 0) {
+        const ssize_t w = pwrite(fd, p, n, (off_t)at);
+        if (w <= 0) return false;
+        p += w;
+        n -= (uint64_t)w;
+        at += (uint64_t)w;
+    }
+    return true;
+}
+
 // Writes the modified ranges and the appended bytes back, with the new end-of-file address.
 void flush(File& f, const std::string& path) {
     if (!f.tail.empty()) {
@@ -959,10 +969,8 @@ void flush(File& f, const std::string& path) {
     const int fd = open(path.c_str(), O_WRONLY);
     if (fd < 0) throw Bad("cannot reopen the file for writing");
     bool ok = true;
-    for (const auto& r : f.dirty)
-        ok = ok && pwrite(fd, f.map + r.first, r.second - r.first, (off_t)r.first) == (ssize_t)(r.second - r.first);
-    if (!f.tail.empty())
-        ok = ok && pwrite(fd, f.tail.data(), f.tail.size(), (off_t)f.size) == (ssize_t)f.tail.size();
+    for (const auto& r : f.dirty) ok = ok && write_at(fd, f.map + r.first, r.second - r.first, r.first);
+    if (!f.tail.empty()) ok = ok && write_at(fd, f.tail.data(), f.tail.size(), f.size);
     ok = close(fd) == 0 && ok;
     if (!ok) throw Bad("short write");
 }
@@ -1035,7 +1043,7 @@ int hpd_h5_write(const char* path, const char* dataset, const int64_t* labels, i
             return fail(HPD_ERR_INVALID, "Could not open dataset " + name);
         }
         const std::vector<unsigned char> b = new_file(parts[0], labels, (uint64_t)n);
-        const bool ok = write(fd, b.data(), b.size()) == (ssize_t)b.size();
+        const bool ok = write_at(fd, b.data(), b.size(), 0);
         if (close(fd) != 0 || !ok)
             return fail(HPD_ERR_RUNTIME, "Failed to write data, target data set is probably of wrong size or type");
         return HPD_OK;
