@@ -579,7 +579,9 @@ int run_pipeline_k(const Request& rq, Arena& main, Timers* tm, RunInfo& info, st
         int pass = 0;
         bool converged = false;
         while (h_left > 0 && !converged) {
-            for (int k = 0; k < kPassesPerCheck; ++k) {
+            // after the first round the values change slowly: decide every 8 passes
+            const int per_check = pass < kPassesPerCheck ? kPassesPerCheck : 2 * kPassesPerCheck;
+            for (int k = 0; k < per_check; ++k) {
                 if (pass >= rq.tie_pass_limit) {
                     err = "border tie-break did not converge";
                     return kTimeout;
