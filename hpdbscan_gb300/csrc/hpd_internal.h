@@ -76,6 +76,15 @@ struct Request {
 constexpr int kDefaultSparseQueries = 8;
 constexpr int kDefaultDenseMinPoints = 128;
 constexpr int kDefaultGreedyTiles = 6;
+// Above the largest size class of the tuned table (10^6 points), for three or more
+// dimensions, measured on the 10M-point 3-D workload on GB300: 12.4 ms per clustering
+// against 13.3 ms with the values above (labels do not depend on them).  The 50M-point
+// 2-D skewed workload was slower with them (core test 28.5 -> 31.2 ms) and keeps the
+// values above.
+constexpr int64_t kLargeInputPoints = 1000000;
+constexpr int kLargeSparseQueries = 16;
+constexpr int kLargeDenseMinPoints = 64;
+constexpr int kLargeGreedyTiles = 12;
 hpd_tuning resolve_tuning(const hpd_tuning& own, int64_t n, int d);
 int set_tuning_table(const hpd_tuning_entry* entries, int32_t n_entries);
 

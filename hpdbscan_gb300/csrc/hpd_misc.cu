@@ -59,9 +59,10 @@ hpd_tuning resolve_tuning(const hpd_tuning& own, int64_t n, int d) {
             }
         }
     }
-    if (!t.sparse_queries) t.sparse_queries = kDefaultSparseQueries;
-    if (!t.dense_min_points) t.dense_min_points = kDefaultDenseMinPoints;
-    if (!t.greedy_tiles) t.greedy_tiles = kDefaultGreedyTiles;
+    const bool large = n > kLargeInputPoints && d >= 3;
+    if (!t.sparse_queries) t.sparse_queries = large ? kLargeSparseQueries : kDefaultSparseQueries;
+    if (!t.dense_min_points) t.dense_min_points = large ? kLargeDenseMinPoints : kDefaultDenseMinPoints;
+    if (!t.greedy_tiles) t.greedy_tiles = large ? kLargeGreedyTiles : kDefaultGreedyTiles;
     t.sparse_queries = std::min(std::max(t.sparse_queries, 0), 32);
     t.dense_min_points = std::max(t.dense_min_points, 32);
     t.greedy_tiles = std::max(t.greedy_tiles, 1);
