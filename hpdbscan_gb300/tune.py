@@ -16,7 +16,9 @@ depend on the shape, and none changes a label:
 For each size class (points in [1e3, 1e4), [1e4, 1e5), [1e5, 1e6], times d = 2..5) the
 tuner clusters sample instances of the batch workload and picks the parameters one at
 a time (coordinate descent from the built-in defaults) by the median device time of
-the whole clustering, checking that every setting gives the same labels.  The table
+the whole clustering, checking that every setting gives the same labels.  Above the
+largest class the library's own values apply (for three or more dimensions: 16, 64
+and 12, measured on the 10M-point 3-D workload).  The table
 is written as JSON; ``load_table`` registers it with the library
 (``hpd_set_tuning_table``), after which every call without a tuning of its own --
 batch and served jobs included -- uses the entry of its size class.
