@@ -74,7 +74,7 @@ struct File {
     std::vector<unsigned char> tail; // appended at `size`
     std::vector<std::pair<uint64_t, uint64_t>> dirty;  // modified [lo, hi) below `size`
     int so = 8, sl = 8;              // size of offsets, size of lengths
-    uint64_t sb = 0, base = 0, eoa = 0;
+    uint64_t sb = 0, base = 0, eoa = 0;  // eoa: from the start of the file
     int sb_version = 0, leaf_k = 4, internal_k = 16;
     uint64_t root_header = kUndef, root_btree = kUndef, root_heap = kUndef;
 
@@ -104,7 +104,7 @@ struct File {
         return p;
     }
     uint64_t alloc(uint64_t bytes) {  // zeroed block at the end of the file, 8-byte aligned
-        uint64_t a = std::max(end(), base + eoa);
+        uint64_t a = std::max(end(), eoa);
         a = (a + 7) & ~7ull;
         tail.resize(a - size + bytes, 0);
         return a - base;
@@ -175,7 +175,9 @@ bool open_file(const std::string& path, File& f, bool writable) {
     } else {
         throw Bad("superblock version " + std::to_string(f.sb_version));
     }
-    if (f.eoa != kUndef && (f.base > f.size || f.eoa > f.size - f.base)) throw Bad("truncated file");
+    // the stored end-of-file address counts from the start of the file (user block
+    // included), unlike every other address, which is relative to the base address
+    if (f.eoa != kUndef && f.eoa > f.size) throw Bad("truncated file");
     return true;
 }
 
@@ -964,7 +966,7 @@ bool write_at(int fd, const unsigned char* p, uint64_t n, uint64_t at) {
 void flush(File& f, const std::string& path) {
     if (!f.tail.empty()) {
         if (f.sb_version > 1) throw Unsupported("growing a file with a checksummed superblock");
-        wr(f.mut(f.sb + 40 + (f.sb_version == 1 ? 4 : 0) - f.base, 8), f.end() - f.base, 8);
+        wr(f.mut(f.sb + 40 + (f.sb_version == 1 ? 4 : 0) - f.base, 8), f.end(), 8);
     }
     const int fd = open(path.c_str(), O_WRONLY);
     if (fd < 0) throw Bad("cannot reopen the file for writing");

@@ -342,15 +342,18 @@ class Reader:
 
     def __init__(self, path):
         with open(path, "rb") as fh:
-            self.b = fh.read()
-        assert self.b[:8] == SIG, "no superblock at 0"
-        assert self.b[8] == 0, "superblock version"
-        self.eof = struct.unpack_from("<Q", self.b, 40)[0]
-        self.root = struct.unpack_from("<Q", self.b, 64)[0]
-        assert struct.unpack_from("<I", self.b, 72)[0] == 1
-        self.root_bt, self.root_heap = struct.unpack_from("<QQ", self.b, 80)
-        self.leaf_k, self.internal_k = struct.unpack_from("<HH", self.b, 16)
-        self.blocks = [(0, 96, "superblock")]
+            raw = fh.read()
+        sb = next(a for a in (0, 512, 1024, 2048, 4096) if raw[a:a + 8] == SIG)
+        assert raw[sb + 8] == 0, "superblock version"
+        self.file_size = len(raw)
+        self.eof = struct.unpack_from("<Q", raw, sb + 40)[0]  # counts from the start of the file
+        base = struct.unpack_from("<Q", raw, sb + 24)[0]
+        self.b = raw[base:]  # addresses below are relative to the base address
+        self.root = struct.unpack_from("<Q", raw, sb + 64)[0]
+        assert struct.unpack_from("<I", raw, sb + 72)[0] == 1
+        self.root_bt, self.root_heap = struct.unpack_from("<QQ", raw, sb + 80)
+        self.leaf_k, self.internal_k = struct.unpack_from("<HH", raw, sb + 16)
+        self.blocks = [(sb - base, 96, "superblock")] if sb >= base else []
 
     def u64(self, a):
         return struct.unpack_from("<Q", self.b, a)[0]
@@ -451,7 +454,7 @@ def check_structure(path, names):
     """Every block the library's writer placed, within the end-of-file address and
     without overlaps; returns the labels of each dataset."""
     r = Reader(path)
-    assert r.eof == len(r.b), "end-of-file address differs from the file size"
+    assert r.eof == r.file_size, "end-of-file address differs from the file size"
     r.blocks.append((r.root, 16 + struct.unpack_from("<I", r.b, r.root + 8)[0], "root header"))
     out = {}
     for i, nm in enumerate(names):
@@ -459,5 +462,5 @@ def check_structure(path, names):
     blocks = sorted(r.blocks)
     for (a0, s0, n0), (a1, s1, n1) in zip(blocks, blocks[1:]):
         assert a0 + s0 <= a1, f"{n0} at {a0}+{s0} overlaps {n1} at {a1}"
-    assert blocks[-1][0] + blocks[-1][1] <= r.eof
+    assert blocks[-1][0] + blocks[-1][1] <= len(r.b)
     return out

@@ -104,16 +104,46 @@ def test_empty_matrix(io, tmp_path):
 
 
 def test_user_block(io, tmp_path):
-    """A superblock after a 512-byte user block; addresses stay relative to it."""
+    """A superblock after a 512-byte user block: addresses are relative to the base
+    address, the end-of-file address counts from the start of the file."""
     p = str(tmp_path / "x.h5")
     a = _points(np.float32)
     H.write_matrix(p, a)
     # relocate: user block of 512 bytes, base address 512 in the superblock
     raw = bytearray(open(p, "rb").read())
     raw[24:32] = (512).to_bytes(8, "little")
+    raw[40:48] = (len(raw) + 512).to_bytes(8, "little")
     with open(p, "wb") as fh:
         fh.write(b"\0" * 512 + raw)
     assert np.array_equal(io.read_hdf5(p, "DATA"), a)
+    io.write_hdf5(p, "CLUSTERS", np.arange(57))
+    assert np.array_equal(io.read_hdf5(p, "DATA"), a)
+    assert np.array_equal(H.read_labels(p, "CLUSTERS"), np.arange(57))
+
+
+MAT73 = None
+try:  # a file written by libhdf5 itself: MATLAB 7.3 format (HDF5 behind a 512-byte user block)
+    import scipy.io.matlab as _m
+    _p = os.path.join(os.path.dirname(_m.__file__), "tests", "data", "testhdf5_7.4_GLNX86.mat")
+    MAT73 = _p if os.path.exists(_p) else None
+except ImportError:
+    pass
+
+
+@pytest.mark.skipif(MAT73 is None, reason="scipy's libhdf5-written test file is not installed")
+def test_file_written_by_libhdf5(io, tmp_path):
+    """scipy's test data holds an HDF5 file written by libhdf5 (MATLAB 7.4, 2008): a
+    user block, superblock v0, the root group as a symbol table whose local heap has
+    a free block, and the 1 x 9 double `testdouble` = 0, pi/4, ..., 2 pi."""
+    got = io.read_hdf5(MAT73, "testdouble")
+    assert got.dtype == np.float64 and got.size == 9
+    assert np.allclose(got.ravel(), np.arange(9) * np.pi / 4)
+    import shutil
+    q = str(tmp_path / "copy.mat")
+    shutil.copy(MAT73, q)
+    io.write_hdf5(q, "CLUSTERS", np.arange(-4, 5))  # a new dataset in libhdf5's root group
+    assert np.array_equal(io.read_hdf5(q, "testdouble"), got)
+    assert np.array_equal(H.read_labels(q, "CLUSTERS"), np.arange(-4, 5))
 
 
 # ------------------------------------------------------------------ errors of the reference
