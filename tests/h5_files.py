@@ -145,7 +145,7 @@ class H5:
     def __init__(self, fmt="earliest", leaf_k=4, internal_k=16):
         self.fmt = fmt
         self.leaf_k, self.internal_k = leaf_k, internal_k
-        self.b = bytearray(96 if fmt == "earliest" else 48)
+        self.b = bytearray(104 if fmt == "earliest" else 48)  # room for a version 1 superblock
 
     def alloc(self, n, align=8):
         a = (len(self.b) + align - 1) // align * align
@@ -185,50 +185,81 @@ class H5:
         self.put(a, struct.pack("<BBHII4x", 1, 0, nmsg, 1, len(body)) + body)
         return a
 
-    def header_v2(self, msgs, split=None):
+    def header_v2(self, msgs, split=None, hflags=0x02):
+        """hflags: bits 0-1 width of the chunk-size field, 0x04 creation order tracked
+        (two more bytes per message header), 0x10 attribute phase change values, 0x20
+        access/modification/change/birth times."""
+        order = bool(hflags & 0x04)
+
         def block(ms):
-            return b"".join(struct.pack("<BHB", t, len(body), fl) + body for t, fl, body in ms)
+            out = b""
+            for i, (t, fl, body) in enumerate(ms):
+                out += struct.pack("<BHB", t, len(body), fl) + (struct.pack("<H", i) if order else b"") + body
+            return out
         first, second = (msgs, []) if split is None else (msgs[:split], msgs[split:])
         body0 = block(first)
-        size0 = len(body0) + (4 + 16 if second else 0)
-        a = self.alloc(6 + 4 + size0 + 4)
+        cont_len = (4 + (2 if order else 0) + 16) if second else 0
+        size0 = len(body0) + cont_len
+        width = 1 << (hflags & 3)
+        prefix = b"OHDR" + bytes([2, hflags])
+        if hflags & 0x20:
+            prefix += struct.pack("<IIII", 1_700_000_000, 1_700_000_001, 1_700_000_002, 1_700_000_003)
+        if hflags & 0x10:
+            prefix += struct.pack("<HH", 8, 6)
+        prefix += size0.to_bytes(width, "little")
+        a = self.alloc(len(prefix) + size0 + 4)
         if second:
             cont = b"OCHK" + block(second)
             cont += struct.pack("<I", lookup3(cont))
             ca = self.raw(cont)
             body0 += block([(0x10, 0, q(ca) + q(len(cont)))])
-        head = b"OHDR" + bytes([2, 0x02]) + struct.pack("<I", size0) + body0  # 4-byte chunk size field
+        head = prefix + body0
         self.put(a, head + struct.pack("<I", lookup3(head)))
         return a
 
-    def header(self, msgs, split=None, pad=0):
+    def header(self, msgs, split=None, pad=0, hflags=0x02):
         if self.fmt == "earliest":
             return self.header_v1(msgs, split, pad)
-        return self.header_v2(msgs, split)
+        return self.header_v2(msgs, split, hflags)
 
     # -- datasets
     def dataset(self, arr: np.ndarray, layout="contiguous", big=False, chunk=None, fill=None, split=None,
-                unwritten=False, dtype_msg=None, space=None, extra=(), chunks_per_node=None):
+                unwritten=False, dtype_msg=None, space=None, extra=(), chunks_per_node=None, layout_version=3,
+                fill_style="new", hflags=0x02):
         arr = np.ascontiguousarray(arr)
         dt = arr.dtype.newbyteorder(">" if big else "<")
         raw = arr.astype(dt).tobytes()
         es = arr.dtype.itemsize
         dims = arr.shape
+        dims_es = b"".join(struct.pack("<I", x) for x in list(dims) + [es])
         if layout == "contiguous":
             addr = UNDEF if unwritten else self.raw(raw, at=2048 if self.fmt == "earliest" and len(self.b) < 2048 else None)
             lay = layout_contiguous(addr, len(raw))
+            if layout_version < 3:  # versions 1 and 2: dimensions with the element size last
+                lay = bytes([layout_version, len(dims) + 1, 1, 0, 0, 0, 0, 0]) + q(addr) + dims_es
         elif layout == "compact":
             lay = layout_compact(raw)
+            if layout_version < 3:
+                lay = (bytes([layout_version, len(dims) + 1, 0, 0, 0, 0, 0, 0]) + dims_es +
+                       struct.pack("<I", len(raw)) + raw)
         else:
             btree = UNDEF if unwritten else self.chunk_btree(arr.astype(dt), chunk, chunks_per_node)
             lay = layout_chunked(btree, chunk, es)
-        fillmsg = (0x05, 1, (fill_v2 if self.fmt == "earliest" else fill_v3)(fill))
+            if layout_version < 3:
+                lay = (bytes([layout_version, len(dims) + 1, 2, 0, 0, 0, 0, 0]) + q(btree) +
+                       b"".join(struct.pack("<I", c) for c in list(chunk) + [es]))
+        if fill_style == "old":  # fill value message of the 1.4 format: size, value
+            fillmsg = (0x04, 1, struct.pack("<I", len(fill or b"")) + (fill or b""))
+        elif fill_style == "v1":  # version 1: the size is always present
+            fillmsg = (0x05, 1, bytes([1, 2, 2, 1 if fill else 0]) + struct.pack("<I", len(fill or b"")) + (fill or b""))
+        else:
+            fillmsg = (0x05, 1, (fill_v2 if self.fmt == "earliest" else fill_v3)(fill))
         msgs = [(0x01, 0, space or (space_v1 if self.fmt == "earliest" else space_v2)(dims)),
                 (0x03, 1, dtype_msg or dtype_message(arr.dtype, big)), fillmsg, (0x08, 0, lay)]
         msgs += list(extra)
         if self.fmt == "earliest":
             msgs.append((0x12, 0, mtime()))
-        return self.header(msgs, split, pad=136 if self.fmt == "earliest" else 0)
+        return self.header(msgs, split, pad=136 if self.fmt == "earliest" else 0, hflags=hflags)
 
     def chunk_btree(self, arr, chunk, per_node=None):
         """v1 B-tree (type 1) over the chunks of arr, edge chunks padded; two levels when
@@ -297,23 +328,37 @@ class H5:
         left, right = node(0, snods[:half]), node(0, snods[half:])
         return node(1, [(snods[half - 1][0], left), (snods[-1][0], right)]), heap
 
-    def group(self, children: dict, **kw):
-        """A group object of this file's format holding {name: header address}."""
+    def group(self, children: dict, link_flags=0x00, dense=False, **kw):
+        """A group object of this file's format holding {name: header address}.
+        link_flags (latest format): 0x08 link type stored, 0x04 creation order stored,
+        0x10 character set stored; dense: the link info names a fractal heap (dense
+        link storage), which this module does not write out."""
         if self.fmt == "earliest":
             bt, hp = self.symbol_table_group(children, **kw)
             return self.header_v1([(0x11, 0, q(bt) + q(hp))]), (bt, hp)
-        msgs = [(0x02, 0, bytes([0, 0]) + q(UNDEF) + q(UNDEF)), (0x0A, 0, bytes([0, 0]))]
-        for nm, addr in children.items():
+        msgs = [(0x02, 0, bytes([0, 0]) + q(4096 if dense else UNDEF) + q(UNDEF)), (0x0A, 0, bytes([0, 0]))]
+        for i, (nm, addr) in enumerate(children.items()):
             enc = nm.encode()
-            msgs.append((0x06, 0, bytes([1, 0x00, len(enc)]) + enc + q(addr)))
+            body = bytes([1, link_flags])
+            if link_flags & 0x08:
+                body += bytes([0])  # hard link
+            if link_flags & 0x04:
+                body += q(i)
+            if link_flags & 0x10:
+                body += bytes([1])  # UTF-8
+            body += bytes([len(enc)]) + enc + q(addr)
+            msgs.append((0x06, 0, body))
         return self.header_v2(msgs), None
 
-    def finish(self, root_children: dict, path, **kw):
+    def finish(self, root_children: dict, path, sb_version=None, **kw):
         root, st = self.group(root_children, **kw)
         eof = len(self.b)
         if self.fmt == "earliest":
             bt, hp = st
-            sb = SIG + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", self.leaf_k, self.internal_k, 0)
+            v = sb_version or 0
+            sb = SIG + bytes([v, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", self.leaf_k, self.internal_k, 0)
+            if v == 1:  # indexed storage internal node K, reserved
+                sb += struct.pack("<HH", 32, 0)
             sb += q(0) + q(UNDEF) + q(eof) + q(UNDEF)
             sb += q(0) + q(root) + struct.pack("<II", 1, 0) + q(bt) + q(hp)
         else:

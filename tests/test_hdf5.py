@@ -349,3 +349,75 @@ def test_lookup3_known_answers():
     assert H.lookup3(b"") == 0xDEADBEEF
     assert H.lookup3(b"Four score and seven years ago", 0) == 0x17770551
     assert H.lookup3(b"Four score and seven years ago", 1) == 0xCD628161
+
+
+# ------------------------------------------------------------------ more of the format
+
+def test_superblock_version_1(io, tmp_path):
+    p = str(tmp_path / "x.h5")
+    a = _points(np.float64)
+    f = H.H5("earliest")
+    f.finish({"DATA": f.dataset(a)}, p, sb_version=1)
+    assert np.array_equal(io.read_hdf5(p, "DATA"), a)
+    io.write_hdf5(p, "CLUSTERS", np.arange(57))  # the end-of-file field sits 4 bytes later
+    assert np.array_equal(io.read_hdf5(p, "DATA"), a)
+    raw = open(p, "rb").read()
+    assert int.from_bytes(raw[44:52], "little") == len(raw)
+
+
+@pytest.mark.parametrize("version", [1, 2])
+@pytest.mark.parametrize("layout", ["contiguous", "compact", "chunked"])
+def test_layout_message_versions_1_and_2(io, tmp_path, version, layout):
+    p = str(tmp_path / "x.h5")
+    a = _points(np.int32, n=23)
+    H.write_matrix(p, a, layout=layout, chunk=(5, 2), layout_version=version)
+    assert np.array_equal(io.read_hdf5(p, "DATA"), a)
+
+
+@pytest.mark.parametrize("style", ["old", "v1"])
+def test_fill_value_message_styles(io, tmp_path, style):
+    p = str(tmp_path / "x.h5")
+    H.write_matrix(p, np.zeros((4, 2), np.int16), unwritten=True, fill=np.int16(-9).tobytes(), fill_style=style)
+    assert np.array_equal(io.read_hdf5(p, "DATA"), np.full((4, 2), -9, np.int16))
+
+
+@pytest.mark.parametrize("hflags", [0x00, 0x01, 0x03, 0x06, 0x22, 0x12, 0x36])
+def test_object_header_v2_variants(io, tmp_path, hflags):
+    """Chunk-size fields of 1/2/4/8 bytes, stored times, attribute phase change values
+    and per-message creation order, with and without a continuation block."""
+    a = _points(np.float32, n=31)
+    for split in (None, 2):
+        p = str(tmp_path / "x.h5")
+        H.write_matrix(p, a, fmt="latest", hflags=hflags, split=split)
+        assert np.array_equal(io.read_hdf5(p, "DATA"), a)
+
+
+@pytest.mark.parametrize("link_flags", [0x08, 0x04, 0x10, 0x1C])
+def test_link_message_variants(io, tmp_path, link_flags):
+    p = str(tmp_path / "x.h5")
+    a = _points(np.uint8, n=12)
+    f = H.H5("latest")
+    kids = {"other": f.dataset(a[:3]), "DATA": f.dataset(a)}
+    f.finish(kids, p, link_flags=link_flags)
+    assert np.array_equal(io.read_hdf5(p, "DATA"), a)
+    assert np.array_equal(io.read_hdf5(p, "other"), a[:3])
+
+
+def test_dense_link_storage_is_reported(io, tmp_path):
+    p = str(tmp_path / "x.h5")
+    f = H.H5("latest")
+    f.finish({"DATA": f.dataset(_points(np.float32))}, p, dense=True)
+    with pytest.raises(ValueError, match=r"^Could not open dataset DATA \(groups with dense link storage\)$"):
+        io.read_hdf5(p, "DATA")
+
+
+def test_shared_datatype_is_reported(io, tmp_path):
+    p = str(tmp_path / "x.h5")
+    f = H.H5("earliest")
+    a = np.zeros((3, 2), np.float32)
+    shared = (0x03, 2, bytes([1, 0, 0, 0]) + H.q(4096))  # flag 2: the message points at a committed type
+    hdr = f.header_v1([(0x01, 0, H.space_v1(a.shape)), shared, (0x05, 1, H.fill_v2()),
+                       (0x08, 0, H.layout_contiguous(f.raw(a.tobytes()), a.nbytes))])
+    f.finish({"DATA": hdr}, p)
+    with pytest.raises(ValueError, match=r"^Could not open dataset DATA \(shared dataspace or datatype messages\)$"):
+        io.read_hdf5(p, "DATA")
