@@ -421,3 +421,23 @@ def test_shared_datatype_is_reported(io, tmp_path):
     f.finish({"DATA": hdr}, p)
     with pytest.raises(ValueError, match=r"^Could not open dataset DATA \(shared dataspace or datatype messages\)$"):
         io.read_hdf5(p, "DATA")
+
+
+def test_write_into_compact_big_endian_and_chunked_targets(io, tmp_path):
+    p = str(tmp_path / "x.h5")
+    f = H.H5("earliest")
+    kids = {"COMPACT": f.dataset(np.zeros((6, 1), np.int64), layout="compact"),
+            "BIG": f.dataset(np.zeros((6, 1), np.int32), big=True),
+            "CHUNKED": f.dataset(np.zeros((6, 1), np.int64), layout="chunked", chunk=(4, 1))}
+    f.finish(kids, p)
+    io.write_hdf5(p, "COMPACT", np.arange(6) - 3)
+    assert np.array_equal(io.read_hdf5(p, "COMPACT")[:, 0], np.arange(6) - 3)
+    io.write_hdf5(p, "BIG", np.array([-5, 70000, 3, 1 << 40, -(1 << 40), 0]))
+    assert np.array_equal(io.read_hdf5(p, "BIG")[:, 0], [-5, 70000, 3, 2**31 - 1, -2**31, 0])
+    with pytest.raises(RuntimeError, match=r"\(writing chunked datasets\)$"):
+        io.write_hdf5(p, "CHUNKED", np.arange(6))
+    q = str(tmp_path / "latest.h5")
+    g = H.H5("latest")
+    g.finish({"COMPACT": g.dataset(np.zeros((6, 1), np.int64), layout="compact")}, q)
+    with pytest.raises(RuntimeError, match=r"\(compact data inside a checksummed object header\)$"):
+        io.write_hdf5(q, "COMPACT", np.arange(6))
